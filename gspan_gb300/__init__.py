@@ -1,0 +1,231 @@
+"""gspan_gb300: GPU frequent-subgraph mining (gSpan, MNI support) for one GB300.
+
+Python view of the C ABI in ``include/gspan_gb300.h``, through ctypes.  The
+mining itself runs in ``_lib/libgspan_gb300.so`` (CUDA, sm_103a); there is no
+CPU fallback, and importing the package fails loudly if the library has not
+been built (``python -m gspan_gb300.build``).
+
+Typical use mirrors the reference's ``fsm(graph, k, min_support)``
+(gspan.h:41 of haozixu/gSpan)::
+
+    from gspan_gb300 import Miner, load_bin, format_pattern
+    g = load_bin("graph.bin")
+    with Miner() as m:
+        patterns, stats = m.fsm(g, k=3, min_support=300)
+    for code, sup in patterns:
+        print(format_pattern(code, sup))
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from .datagen import CSR, load_bin  # noqa: F401  (re-exported)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libgspan_gb300.so")
+BIN_DIR = os.path.join(_HERE, "_lib")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        f"gspan_gb300: native library missing at {LIB_PATH}; build it with `python -m gspan_gb300.build` "
+        "(there is no CPU fallback)")
+
+_lib = ctypes.CDLL(LIB_PATH)
+
+GSPAN_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "LIMIT", 5: "DEVICE", 6: "ABORTED",
+                7: "NO_DEVICE"}
+
+
+class GspanError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str = ""):
+        self.status = status
+        msg = f"{what}: {STATUS_NAMES.get(status, status)}"
+        if detail:
+            msg += f" ({detail})"
+        super().__init__(msg)
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("domain_mode", ctypes.c_int32),
+                ("hash_threshold", ctypes.c_double), ("mem_fraction", ctypes.c_double),
+                ("profile", ctypes.c_int32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("seeds", ctypes.c_uint64), ("extended", ctypes.c_uint64), ("patterns", ctypes.c_uint64),
+                ("support_keys", ctypes.c_uint64), ("hash_domains", ctypes.c_uint64),
+                ("scanned_entries", ctypes.c_uint64), ("materialized_rows", ctypes.c_uint64),
+                ("kernel_launches", ctypes.c_uint64), ("levels", ctypes.c_int32), ("mine_ms", ctypes.c_double),
+                ("expand_ms", ctypes.c_double), ("expand_launches", ctypes.c_uint64),
+                ("expand_bytes", ctypes.c_double), ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class PatternEdge(ctypes.Structure):
+    _fields_ = [("frm", ctypes.c_int32), ("to", ctypes.c_int32), ("from_label", ctypes.c_int32),
+                ("edge_label", ctypes.c_int32), ("to_label", ctypes.c_int32)]
+
+
+EMIT_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(PatternEdge), ctypes.c_int32,
+                           ctypes.c_int32)
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_lib.gspan_opts_default.argtypes = [ctypes.POINTER(Opts)]
+_lib.gspan_opts_default.restype = None
+_lib.gspan_ctx_create.argtypes = [ctypes.POINTER(Opts), ctypes.POINTER(ctypes.c_void_p)]
+_lib.gspan_ctx_create.restype = ctypes.c_int
+_lib.gspan_ctx_destroy.argtypes = [ctypes.c_void_p]
+_lib.gspan_ctx_destroy.restype = None
+_lib.gspan_graph_upload.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+_lib.gspan_graph_upload.restype = ctypes.c_int
+_lib.gspan_graph_free.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+_lib.gspan_graph_free.restype = ctypes.c_int
+_lib.gspan_mine.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, EMIT_FN,
+                            ctypes.c_void_p, ctypes.POINTER(Stats)]
+_lib.gspan_mine.restype = ctypes.c_int
+_lib.gspan_is_canonical.argtypes = [ctypes.POINTER(PatternEdge), ctypes.c_int32, _i32p]
+_lib.gspan_is_canonical.restype = ctypes.c_int
+_lib.gspan_status_string.argtypes = [ctypes.c_int]
+_lib.gspan_status_string.restype = ctypes.c_char_p
+_lib.gspan_last_error.argtypes = [ctypes.c_void_p]
+_lib.gspan_last_error.restype = ctypes.c_char_p
+_lib.gspan_max_pattern_edges.argtypes = []
+_lib.gspan_max_pattern_edges.restype = ctypes.c_int32
+
+# Every symbol include/gspan_gb300.h declares (checked by the tests).
+ABI_SYMBOLS = ("gspan_opts_default", "gspan_ctx_create", "gspan_ctx_destroy", "gspan_graph_upload",
+               "gspan_graph_free", "gspan_mine", "gspan_is_canonical", "gspan_status_string",
+               "gspan_last_error", "gspan_max_pattern_edges")
+
+Code = tuple  # tuple of (from, to, from_label, edge_label, to_label)
+
+
+def max_pattern_edges() -> int:
+    return int(_lib.gspan_max_pattern_edges())
+
+
+def is_canonical(code: Sequence[Sequence[int]]) -> bool:
+    """The reference's minimum-DFS-code test (gspan.cu:586-606), host side."""
+    arr = (PatternEdge * len(code))(*[PatternEdge(*map(int, e)) for e in code])
+    out = ctypes.c_int32(0)
+    rc = _lib.gspan_is_canonical(arr, len(code), ctypes.byref(out))
+    if rc != GSPAN_OK:
+        raise GspanError(rc, "gspan_is_canonical")
+    return bool(out.value)
+
+
+def format_pattern(code: Iterable[Sequence[int]], support: int) -> str:
+    """One output line in the reference's format (gspan.cu:67-77)."""
+    return "".join(f"({a} {b} {c} {d} {e})" for a, b, c, d, e in code) + f": {support}"
+
+
+@dataclass
+class DeviceGraph:
+    handle: ctypes.c_void_p
+    n: int
+    m: int
+
+
+class Miner:
+    """One mining context on one GPU (a CUDA stream and the device memory it owns)."""
+
+    def __init__(self, device: int = 0, domain_mode: int = 0, hash_threshold: float = 1.0,
+                 profile: bool = False, mem_fraction: float = 0.85):
+        opts = Opts()
+        _lib.gspan_opts_default(ctypes.byref(opts))
+        opts.device = device
+        opts.domain_mode = domain_mode
+        opts.hash_threshold = hash_threshold
+        opts.profile = 1 if profile else 0
+        opts.mem_fraction = mem_fraction
+        self._ctx = ctypes.c_void_p()
+        rc = _lib.gspan_ctx_create(ctypes.byref(opts), ctypes.byref(self._ctx))
+        if rc != GSPAN_OK:
+            raise GspanError(rc, "gspan_ctx_create")
+        self._graphs: list[DeviceGraph] = []
+
+    def _err(self, rc: int, what: str) -> GspanError:
+        detail = _lib.gspan_last_error(self._ctx) if self._ctx else b""
+        return GspanError(rc, what, (detail or b"").decode())
+
+    def upload(self, g: CSR) -> DeviceGraph:
+        off = np.ascontiguousarray(g.offsets, dtype=np.int32)
+        vl = np.ascontiguousarray(g.vlabels, dtype=np.int32)
+        ed = np.ascontiguousarray(g.edges, dtype=np.int32).reshape(-1, 3)
+        return self.upload_arrays(off, vl, ed)
+
+    def upload_arrays(self, offsets, vlabels, edges) -> DeviceGraph:
+        """Host arrays (numpy, or anything exposing a contiguous int32 buffer
+        through ``.ctypes.data`` or ``.data_ptr()``) in the reference's CSR layout."""
+        def ptr(a):
+            return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        n = int(vlabels.shape[0])
+        m = int(edges.shape[0])
+        h = ctypes.c_void_p()
+        rc = _lib.gspan_graph_upload(self._ctx, n, m, ptr(offsets), ptr(vlabels) if n else None,
+                                     ptr(edges) if m else None, ctypes.byref(h))
+        if rc != GSPAN_OK:
+            raise self._err(rc, "gspan_graph_upload")
+        dg = DeviceGraph(h, n, m)
+        self._graphs.append(dg)
+        return dg
+
+    def free(self, dg: DeviceGraph) -> None:
+        if dg in self._graphs:
+            self._graphs.remove(dg)
+            rc = _lib.gspan_graph_free(self._ctx, dg.handle)
+            if rc != GSPAN_OK:
+                raise self._err(rc, "gspan_graph_free")
+
+    def mine(self, dg: DeviceGraph, k: int, min_support: int):
+        """Returns (patterns, stats): patterns as [(code, support)] in the
+        reference's pre-order, code a tuple of 5-tuples."""
+        out: list = []
+
+        def emit(_user, code, length, support):
+            out.append((tuple((code[i].frm, code[i].to, code[i].from_label, code[i].edge_label,
+                               code[i].to_label) for i in range(length)), int(support)))
+            return 0
+
+        cb = EMIT_FN(emit)
+        st = Stats()
+        rc = _lib.gspan_mine(self._ctx, dg.handle, int(k), int(min_support), cb, None, ctypes.byref(st))
+        if rc != GSPAN_OK:
+            raise self._err(rc, "gspan_mine")
+        return out, st.as_dict()
+
+    def fsm(self, g: CSR, k: int, min_support: int):
+        """Upload, mine, free: the reference's ``fsm`` as one call."""
+        dg = self.upload(g)
+        try:
+            return self.mine(dg, k, min_support)
+        finally:
+            self.free(dg)
+
+    def close(self) -> None:
+        for dg in list(self._graphs):
+            self.free(dg)
+        if self._ctx:
+            _lib.gspan_ctx_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

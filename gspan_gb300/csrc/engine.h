@@ -1,0 +1,134 @@
+// Internal declarations shared by the host orchestration (miner.cc, capi.cc)
+// and the CUDA kernels (kernels.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "gspan_gb300.h"
+
+namespace gs {
+
+// Largest pattern (in edges) the kernels handle; a pattern of E edges has at
+// most E+1 vertices.  Row images and per-source state live in shared memory
+// sized by kMaxV.
+constexpr int kMaxE = 15;
+constexpr int kMaxV = kMaxE + 1;
+
+// Packed adjacency entry: (edge-label rank << 48) | (to-label rank << 32) | to.
+// Each vertex's entries are sorted ascending, i.e. by (edge label, to label, to).
+__host__ __device__ inline uint64_t pack_entry(uint32_t el, uint32_t tl, uint32_t to)
+{
+    return ((uint64_t)el << 48) | ((uint64_t)tl << 32) | (uint64_t)to;
+}
+__host__ __device__ inline uint32_t entry_to(uint64_t e) { return (uint32_t)e; }
+__host__ __device__ inline uint32_t entry_tl(uint64_t e) { return (uint32_t)(e >> 32) & 0xFFFFu; }
+__host__ __device__ inline uint32_t entry_el(uint64_t e) { return (uint32_t)(e >> 48); }
+
+// Device-side status word bits (set by kernels, read by the host after a pass).
+enum : uint32_t {
+    kErrHashFull = 1u << 0,     // a hashset probe ran through its whole table
+    kErrBadGraph = 1u << 1,     // upload validation: offsets or entries inconsistent
+    kErrCursor = 1u << 2,       // a materialisation cursor ran past its reserved rows
+};
+
+// The graph in HBM.  Labels are replaced by their rank among the distinct
+// labels present, which preserves every `<` / `<=` test of the reference.
+struct DevGraph {
+    int32_t n = 0;              // vertices
+    int32_t m = 0;              // directed entries (2 per undirected edge)
+    int32_t nvl = 0, nel = 0;   // distinct vertex / edge labels
+    int32_t* offsets = nullptr; // [n+1]
+    uint64_t* adj = nullptr;    // [m] packed entries, sorted per vertex
+    int32_t* src = nullptr;     // [m] owning vertex of each entry
+    int32_t* vrank = nullptr;   // [n] vertex label rank
+    std::vector<int32_t> vlabel_of_rank, elabel_of_rank;
+};
+
+// Where a domain (set of graph vertices that one pattern vertex maps to)
+// lives: `nvc` consecutive tables of `cap` 32-bit words starting at `off` in
+// the domain pool.  Bitmap: cap = ceil(n/32) words.  Hashset: cap = power of
+// two slots holding vertex ids, empty = 0xFFFFFFFF.
+struct DomDesc {
+    uint64_t off;
+    uint32_t cap;
+    uint16_t nvc;
+    uint16_t hash;
+};
+
+constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
+
+// One parent pattern of an extension level, as the kernels see it.
+// Sources: s = 0 is the first-forward source v_n; s >= 1 are the tails of the
+// rightmost-path edges rmpath[s-1] (other-forward), each with the (edge label,
+// to label) lower bound (src_el, src_tl) of gspan.cu:464-483.
+// Backward targets t: rmpath[t+1] tails (gspan.cu:702-711), with the label test
+// of gspan.cu:437-439 reduced to: edge label > back_el, or == back_el when
+// back_eq is set.
+struct ParentMeta {
+    int64_t row_begin;          // first row in the level table
+    int64_t row_end;
+    int64_t tile_begin;         // first 32-row tile index of this parent
+    int32_t key_base;           // first key of this parent in the level key space
+    int16_t nv;                 // pattern vertices
+    int16_t nsrc;
+    int16_t nback;
+    int16_t nedge;
+    int16_t vn;                 // rightmost vertex v_n
+    int16_t min_label;          // vertex-label rank of v0
+    int16_t vlab[kMaxV];        // vertex-label rank of each pattern vertex
+    int16_t src_v[kMaxV];
+    int16_t src_el[kMaxV];
+    int16_t src_tl[kMaxV];
+    int16_t back_v[kMaxV];
+    int16_t back_el[kMaxV];
+    int16_t back_eq[kMaxV];
+    int8_t e_from[kMaxE];       // parent code edges, for the has_edge test
+    int8_t e_to[kMaxE];
+    int16_t e_el[kMaxE];
+};
+
+// Per-level key space arrays on the device.
+struct LevelKeys {
+    unsigned long long* counts = nullptr;   // [nkeys]
+    int32_t* act = nullptr;                 // [nkeys] active-key index or -1
+    DomDesc* dom = nullptr;                 // [nact]
+    long long* mat_off = nullptr;           // [nact] first output row, or -1
+    unsigned long long* cursor = nullptr;   // [nact]
+};
+
+enum class Pass : int { Count = 0, Support = 1 };
+
+struct ExpandArgs {
+    const DevGraph* g;                 // host copy; device pointers inside are used
+    const ParentMeta* parents;         // device
+    int32_t nparents;
+    int64_t ntiles;
+    int32_t in_cols;                   // columns of the parent table
+    int32_t* const* in_col_ptrs;       // device array [in_cols] of column pointers
+    int32_t* const* out_col_ptrs;      // device array [out_cols] (support pass with materialisation)
+    LevelKeys keys;
+    uint32_t* dom_pool;
+    unsigned long long* tile_counter;  // device scratch, zeroed before launch
+    unsigned long long* scanned;       // device accumulator of adjacency entries read
+    uint32_t* status;
+};
+
+// Kernel launchers (kernels.cu).  All are asynchronous on `st`.
+cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d_edges,
+                                   const int32_t* d_vrank_of_vertex, const int32_t* d_elabels_sorted,
+                                   int32_t nel, DevGraph& g, uint64_t* d_tmp, uint32_t* d_status,
+                                   cudaStream_t st);
+cudaError_t launch_seed_count(const DevGraph& g, unsigned long long* counts, cudaStream_t st);
+cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* pool, int32_t* col0,
+                                int32_t* col1, uint32_t* status, cudaStream_t st);
+cudaError_t launch_expand(const ExpandArgs& a, Pass pass, cudaStream_t st);
+cudaError_t launch_domain_sizes(const DomDesc* dom, int32_t nact, const uint32_t* pool,
+                                uint32_t* sizes /* [nact * kMaxV] */, cudaStream_t st);
+
+int expand_grid_blocks(int device);
+
+}  // namespace gs

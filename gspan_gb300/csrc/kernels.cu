@@ -1,0 +1,543 @@
+// CUDA kernels of the miner, written for sm_103a.
+//
+// Everything here is integer work on the graph store and on column-oriented
+// embedding tables; none of it is a dense contraction, so tensor cores are not
+// used.  The bounds are HBM / L2 bandwidth (adjacency and table streams) and
+// L2 atomic throughput (domain sets).
+//
+//  * build_adjacency : packs every CSR entry as (edge label, to label, to) and
+//                      sorts each vertex's entries by that key (warp per vertex).
+//  * seed_count / seed_support : 1-edge patterns (gspan.cu:411-426, 1176-1190).
+//  * expand          : one pass over the embeddings of every parent pattern of a
+//                      level, evaluating the backward / first-forward /
+//                      other-forward rules of gspan.cu:428-483 for each
+//                      (embedding, adjacency entry) pair.  Pass::Count builds the
+//                      histogram of child DFS-code tuples; Pass::Support fills
+//                      the MNI domains of the active tuples and, when the level
+//                      is not the last, scatters the child rows grouped by tuple
+//                      (a one-digit counting sort whose offsets the host derived
+//                      from the Count histogram).
+//  * domain_sizes    : popcount / occupied-slot count of every domain.
+#include "engine.h"
+
+namespace gs {
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr int kExpandWarps = 8;
+constexpr int kExpandThreads = kExpandWarps * 32;
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ---------------------------------------------------------------------------
+// Domain sets.
+
+__device__ __forceinline__ void bitmap_insert(uint32_t* words, uint32_t v)
+{
+    uint32_t* w = words + (v >> 5);
+    const uint32_t bit = 1u << (v & 31u);
+    // Bits only go 0 -> 1, so a stale read can cost an extra atomic but never
+    // loses an insert.  __ldcg reads L2, where the atomics land.
+    if (!(__ldcg(w) & bit)) atomicOr(w, bit);
+}
+
+__device__ __forceinline__ uint32_t hash_slot(uint32_t v, uint32_t cap)
+{
+    // Fibonacci hashing scaled to [0, cap) by a 32x32->64 multiply.
+    return (uint32_t)(((uint64_t)(v * 2654435769u) * cap) >> 32);
+}
+
+__device__ void hash_insert(uint32_t* table, uint32_t cap, uint32_t v, uint32_t* status)
+{
+    uint32_t slot = hash_slot(v, cap);
+    for (uint32_t probe = 0; probe < cap; ++probe) {
+        uint32_t cur = __ldcg(table + slot);
+        if (cur == v) return;
+        if (cur == kHashEmpty) {
+            cur = atomicCAS(table + slot, kHashEmpty, v);
+            if (cur == kHashEmpty || cur == v) return;
+        }
+        slot = (slot + 1u) & (cap - 1u);
+    }
+    atomicOr(status, kErrHashFull);   // capacity is >= 2x the largest possible size: unreachable
+}
+
+__device__ __forceinline__ void dom_insert(uint32_t* pool, const DomDesc& d, int p, uint32_t v, uint32_t* status)
+{
+    uint32_t* base = pool + d.off + (uint64_t)p * d.cap;
+    if (d.hash)
+        hash_insert(base, d.cap, v, status);
+    else
+        bitmap_insert(base, v);
+}
+
+// First index in adj[b, e) whose packed key is >= key.
+__device__ __forceinline__ int32_t lower_bound_entry(const uint64_t* __restrict__ adj, int32_t b, int32_t e, uint64_t key)
+{
+    while (b < e) {
+        const int32_t mid = b + ((e - b) >> 1);
+        if (__ldg(adj + mid) < key)
+            b = mid + 1;
+        else
+            e = mid;
+    }
+    return b;
+}
+
+// ---------------------------------------------------------------------------
+// Graph store build.
+
+__global__ void k_entry_keys(int32_t m, int32_t n, const gspan_edge* __restrict__ edges,
+                             const int32_t* __restrict__ vrank, const int32_t* __restrict__ elabels,
+                             int32_t nel, uint64_t* __restrict__ keys, uint32_t* status)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const gspan_edge e = edges[i];
+        if (e.to < 0 || e.to >= n) {
+            atomicOr(status, kErrBadGraph);
+            keys[i] = 0;
+            continue;
+        }
+        int32_t lo = 0, hi = nel - 1;
+        while (lo < hi) {
+            const int32_t mid = (lo + hi) >> 1;
+            if (elabels[mid] < e.label) lo = mid + 1; else hi = mid;
+        }
+        keys[i] = pack_entry((uint32_t)lo, (uint32_t)vrank[e.to], (uint32_t)e.to);
+    }
+}
+
+// Warp per vertex: every entry's final slot is its rank inside the segment
+// (ties broken by original position), so the sort is stable and needs no
+// scratch beyond the unsorted keys.
+__global__ void k_sort_segments(int32_t n, int32_t m, const int32_t* __restrict__ offsets,
+                                const gspan_edge* __restrict__ edges, const uint64_t* __restrict__ keys,
+                                uint64_t* __restrict__ adj, int32_t* __restrict__ src, uint32_t* status)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = warp; v < n; v += nwarps) {
+        const int32_t b = offsets[v], e = offsets[v + 1];
+        if (b < 0 || e < b || e > m) {
+            if (lane == 0) atomicOr(status, kErrBadGraph);
+            continue;
+        }
+        for (int32_t j = b + lane; j < e; j += 32) {
+            if (edges[j].from != (int32_t)v) atomicOr(status, kErrBadGraph);
+            const uint64_t kj = __ldg(keys + j);
+            int32_t rank = 0;
+            for (int32_t i = b; i < e; ++i) {
+                const uint64_t ki = __ldg(keys + i);
+                rank += (ki < kj) || (ki == kj && i < j);
+            }
+            adj[b + rank] = kj;
+            src[j] = (int32_t)v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Seeds: every directed entry u->w with label(u) <= label(w) is an embedding of
+// the 1-edge code (0,1,label(u),edge label,label(w)).
+
+__device__ __forceinline__ bool seed_key(const int32_t* __restrict__ src, const uint64_t* __restrict__ adj,
+                                         const int32_t* __restrict__ vrank, int32_t nvl, int32_t nel, int64_t i,
+                                         int32_t* key, uint32_t* u, uint32_t* w)
+{
+    const uint64_t e = adj[i];
+    *u = (uint32_t)src[i];
+    *w = entry_to(e);
+    const int32_t fl = vrank[*u];
+    const int32_t tl = (int32_t)entry_tl(e);
+    *key = (fl * nel + (int32_t)entry_el(e)) * nvl + tl;
+    return fl <= tl;
+}
+
+__global__ void k_seed_count(int32_t m, const int32_t* __restrict__ src, const uint64_t* __restrict__ adj,
+                             const int32_t* __restrict__ vrank, int32_t nvl, int32_t nel,
+                             unsigned long long* __restrict__ counts)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < m; base += nwarps * 32) {
+        const int64_t i = base + lane;
+        int32_t key = 0;
+        uint32_t u, w;
+        const bool ok = i < m && seed_key(src, adj, vrank, nvl, nel, i, &key, &u, &w);
+        const unsigned mask = __ballot_sync(kFull, ok);
+        if (ok) {
+            const unsigned peers = __match_any_sync(mask, key);
+            if (lane == __ffs(peers) - 1) atomicAdd(counts + key, (unsigned long long)__popc(peers));
+        }
+    }
+}
+
+__global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const uint64_t* __restrict__ adj,
+                               const int32_t* __restrict__ vrank, int32_t nvl, int32_t nel, LevelKeys keys,
+                               uint32_t* __restrict__ pool, int32_t* __restrict__ col0, int32_t* __restrict__ col1,
+                               uint32_t* status)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < m; base += nwarps * 32) {
+        const int64_t i = base + lane;
+        int32_t key = 0;
+        uint32_t u = 0, w = 0;
+        bool ok = i < m && seed_key(src, adj, vrank, nvl, nel, i, &key, &u, &w);
+        const int32_t a = ok ? keys.act[key] : -1;
+        ok = a >= 0;
+        if (ok) {
+            const DomDesc d = keys.dom[a];
+            dom_insert(pool, d, 0, u, status);
+            dom_insert(pool, d, 1, w, status);
+        }
+        const bool mat = ok && keys.mat_off[a] >= 0;
+        const unsigned mm = __ballot_sync(kFull, mat);
+        if (mat) {
+            const unsigned peers = __match_any_sync(mm, a);
+            const int leader = __ffs(peers) - 1;
+            unsigned long long at = 0;
+            if (lane == leader) at = atomicAdd(keys.cursor + a, (unsigned long long)__popc(peers));
+            at = __shfl_sync(mm, at, leader);
+            const long long row = keys.mat_off[a] + (long long)at + __popc(peers & lanemask_lt());
+            col0[row] = (int32_t)u;
+            col1[row] = (int32_t)w;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Extension.
+
+struct ExpandDev {
+    const int32_t* offsets;
+    const uint64_t* adj;
+    int32_t nvl, nel;
+    const ParentMeta* parents;
+    int32_t nparents;
+    int64_t ntiles;
+    int32_t* const* in_cols;
+    int32_t* const* out_cols;
+    LevelKeys keys;
+    uint32_t* pool;
+    unsigned long long* tile_counter;
+    unsigned long long* scanned;
+    uint32_t* status;
+};
+
+struct WarpScratch {
+    int32_t img[32][kMaxV + 1];   // this tile's row images, one row per lane
+    int32_t start[32][kMaxV];     // per row and source: first adjacency entry in range
+    int32_t cnt[32][kMaxV];       // per row and source: entries in range
+    int32_t pre[32];              // exclusive prefix of the rows' entry counts
+};
+
+template <Pass kPass>
+__global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    WarpScratch& W = reinterpret_cast<WarpScratch*>(smem_raw)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int32_t LeLv = a.nel * a.nvl;
+
+    for (;;) {
+        long long tile = 0;
+        if (lane == 0) tile = (long long)atomicAdd(a.tile_counter, 1ull);
+        tile = __shfl_sync(kFull, tile, 0);
+        if (tile >= a.ntiles) break;
+
+        // Parent owning this tile: last parent whose first tile is <= tile.
+        int32_t lo = 0, hi = a.nparents - 1;
+        while (lo < hi) {
+            const int32_t mid = (lo + hi + 1) >> 1;
+            if (a.parents[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+        }
+        const ParentMeta& P = a.parents[lo];
+        const int nv = P.nv, nsrc = P.nsrc, nback = P.nback;
+        const int32_t key_base = P.key_base;
+        const int min_label = P.min_label;
+        const int64_t row = P.row_begin + (tile - P.tile_begin) * 32 + lane;
+        const bool live = row < P.row_end;
+
+        for (int p = 0; p < nv; ++p) W.img[lane][p] = live ? __ldcs(a.in_cols[p] + row) : -1;
+
+        int32_t work = 0;
+        for (int s = 0; s < nsrc; ++s) {
+            int32_t st = 0, c = 0;
+            if (live) {
+                const int32_t u = W.img[lane][P.src_v[s]];
+                const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
+                const uint64_t lo_key = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
+                                               : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
+                st = lower_bound_entry(a.adj, b, e, lo_key);
+                c = e - st;
+            }
+            W.start[lane][s] = st;
+            W.cnt[lane][s] = c;
+            work += c;
+        }
+        int32_t incl = work;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t t = __shfl_up_sync(kFull, incl, d);
+            if (lane >= d) incl += t;
+        }
+        W.pre[lane] = incl - work;
+        const int32_t total = __shfl_sync(kFull, incl, 31);
+        __syncwarp();
+        if (kPass == Pass::Count && lane == 0 && total > 0)
+            atomicAdd(a.scanned, (unsigned long long)total);
+
+        // Backward candidates: at most one per (row, rightmost-path target).
+        for (int t = 0; t < nback; ++t) {
+            bool ok = false;
+            int32_t bel = 0;
+            if (live) {
+                const int bv = P.back_v[t];
+                const int32_t x = W.img[lane][bv];
+                const int32_t un = W.img[lane][P.vn];
+                const uint32_t tlx = (uint32_t)P.vlab[bv];
+                const int32_t b = __ldg(a.offsets + un), e = __ldg(a.offsets + un + 1);
+                for (int32_t el = P.back_eq[t] ? P.back_el[t] : P.back_el[t] + 1; el < a.nel && !ok; ++el) {
+                    const uint64_t want = pack_entry((uint32_t)el, tlx, (uint32_t)x);
+                    const int32_t pos = lower_bound_entry(a.adj, b, e, want);
+                    if (pos < e && __ldg(a.adj + pos) == want) {
+                        bool used = false;
+                        for (int j = 0; j < P.nedge; ++j) {
+                            if (P.e_el[j] != el) continue;
+                            const int32_t f = W.img[lane][P.e_from[j]], g2 = W.img[lane][P.e_to[j]];
+                            if ((f == un && g2 == x) || (g2 == un && f == x)) used = true;
+                        }
+                        if (!used) {
+                            ok = true;
+                            bel = el;
+                        }
+                    }
+                }
+            }
+            const int32_t key = key_base + nsrc * LeLv + t * a.nel + bel;
+            const unsigned mask = __ballot_sync(kFull, ok);
+            if (kPass == Pass::Count) {
+                if (ok) {
+                    const unsigned peers = __match_any_sync(mask, key);
+                    if (lane == __ffs(peers) - 1) atomicAdd(a.keys.counts + key, (unsigned long long)__popc(peers));
+                }
+            } else {
+                const int32_t ai = ok ? a.keys.act[key] : -1;
+                const bool sup = ai >= 0;
+                DomDesc d{};
+                if (sup) {
+                    d = a.keys.dom[ai];
+                    for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)W.img[lane][p], a.status);
+                }
+                const bool mat = sup && a.keys.mat_off[ai] >= 0;
+                const unsigned mm = __ballot_sync(kFull, mat);
+                if (mat) {
+                    const unsigned peers = __match_any_sync(mm, ai);
+                    const int leader = __ffs(peers) - 1;
+                    unsigned long long at = 0;
+                    if (lane == leader) at = atomicAdd(a.keys.cursor + ai, (unsigned long long)__popc(peers));
+                    at = __shfl_sync(mm, at, leader);
+                    const long long r = a.keys.mat_off[ai] + (long long)at + __popc(peers & lanemask_lt());
+                    for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[lane][p];
+                }
+            }
+        }
+
+        // Forward candidates: the tile's adjacency ranges, 32 entries at a time.
+        for (int32_t base = 0; base < total; base += 32) {
+            const int32_t item = base + lane;
+            bool ok = item < total;
+            int owner = 0;
+            uint32_t to = 0;
+            int32_t key = 0;
+            if (ok) {
+                int l2 = 0, h2 = 31;
+                while (l2 < h2) {
+                    const int mid = (l2 + h2 + 1) >> 1;
+                    if (W.pre[mid] <= item) l2 = mid; else h2 = mid - 1;
+                }
+                owner = l2;
+                int32_t j = item - W.pre[owner];
+                int s = 0;
+                while (j >= W.cnt[owner][s]) {
+                    j -= W.cnt[owner][s];
+                    ++s;
+                }
+                const uint64_t e = __ldg(a.adj + W.start[owner][s] + j);
+                to = entry_to(e);
+                const int32_t tl = (int32_t)entry_tl(e);
+                bool fresh = tl >= min_label;
+                for (int p = 0; p < nv; ++p) fresh &= W.img[owner][p] != (int32_t)to;
+                ok = fresh;
+                key = key_base + s * LeLv + (int32_t)entry_el(e) * a.nvl + tl;
+            }
+            const unsigned mask = __ballot_sync(kFull, ok);
+            if (kPass == Pass::Count) {
+                if (ok) {
+                    const unsigned peers = __match_any_sync(mask, key);
+                    if (lane == __ffs(peers) - 1) atomicAdd(a.keys.counts + key, (unsigned long long)__popc(peers));
+                }
+            } else {
+                const int32_t ai = ok ? a.keys.act[key] : -1;
+                const bool sup = ai >= 0;
+                const unsigned sm = __ballot_sync(kFull, sup);
+                DomDesc d{};
+                if (sup) {
+                    d = a.keys.dom[ai];
+                    dom_insert(a.pool, d, nv, to, a.status);
+                    // The parent row's images go in once per (row, child tuple) in this chunk.
+                    const unsigned peers = __match_any_sync(sm, ((unsigned long long)owner << 32) | (unsigned)ai);
+                    if (lane == __ffs(peers) - 1)
+                        for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)W.img[owner][p], a.status);
+                }
+                const bool mat = sup && a.keys.mat_off[ai] >= 0;
+                const unsigned mm = __ballot_sync(kFull, mat);
+                if (mat) {
+                    const unsigned peers = __match_any_sync(mm, ai);
+                    const int leader = __ffs(peers) - 1;
+                    unsigned long long at = 0;
+                    if (lane == leader) at = atomicAdd(a.keys.cursor + ai, (unsigned long long)__popc(peers));
+                    at = __shfl_sync(mm, at, leader);
+                    const long long r = a.keys.mat_off[ai] + (long long)at + __popc(peers & lanemask_lt());
+                    for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[owner][p];
+                    a.out_cols[nv][r] = (int32_t)to;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Block per (active tuple, pattern vertex): the size of that domain.
+__global__ void k_domain_sizes(const DomDesc* __restrict__ dom, const uint32_t* __restrict__ pool,
+                               uint32_t* __restrict__ sizes)
+{
+    const int32_t ai = blockIdx.x / kMaxV;
+    const int p = blockIdx.x % kMaxV;
+    const DomDesc d = dom[ai];
+    if (p >= d.nvc) return;
+    const uint32_t* base = pool + d.off + (uint64_t)p * d.cap;
+    uint32_t c = 0;
+    for (uint32_t i = threadIdx.x; i < d.cap; i += blockDim.x) {
+        const uint32_t w = base[i];
+        c += d.hash ? (w != kHashEmpty) : __popc(w);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(kFull, c, o);
+    __shared__ uint32_t part[32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        c = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(kFull, c, o);
+        if (threadIdx.x == 0) sizes[blockIdx.x] = c;
+    }
+}
+
+int grid_for(int64_t work, int threads)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (work + threads - 1) / threads;
+    const int64_t cap = (int64_t)sms * 16;
+    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+}  // namespace
+
+cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d_edges,
+                                   const int32_t* d_vrank_of_vertex, const int32_t* d_elabels_sorted,
+                                   int32_t nel, DevGraph& g, uint64_t* d_tmp, uint32_t* d_status,
+                                   cudaStream_t st)
+{
+    if (g.m > 0) {
+        k_entry_keys<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.n, d_edges, d_vrank_of_vertex, d_elabels_sorted,
+                                                         nel, d_tmp, d_status);
+    }
+    if (g.n > 0) {
+        k_sort_segments<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, d_offsets, d_edges, d_tmp,
+                                                                          g.adj, g.src, d_status);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seed_count(const DevGraph& g, unsigned long long* counts, cudaStream_t st)
+{
+    if (g.m == 0) return cudaSuccess;
+    k_seed_count<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.nvl, g.nel, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* pool, int32_t* col0, int32_t* col1,
+                                uint32_t* status, cudaStream_t st)
+{
+    if (g.m == 0) return cudaSuccess;
+    k_seed_support<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.nvl, g.nel, keys, pool,
+                                                       col0, col1, status);
+    return cudaGetLastError();
+}
+
+int expand_grid_blocks(int device)
+{
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const size_t smem = sizeof(WarpScratch) * kExpandWarps;
+    cudaFuncSetAttribute(k_expand<Pass::Count>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_expand<Pass::Support>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_expand<Pass::Support>, kExpandThreads, smem);
+    if (per_sm < 1) per_sm = 1;
+    return sms * per_sm;
+}
+
+cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
+{
+    if (x.ntiles == 0) return cudaSuccess;
+    ExpandDev a;
+    a.offsets = x.g->offsets;
+    a.adj = x.g->adj;
+    a.nvl = x.g->nvl;
+    a.nel = x.g->nel;
+    a.parents = x.parents;
+    a.nparents = x.nparents;
+    a.ntiles = x.ntiles;
+    a.in_cols = x.in_col_ptrs;
+    a.out_cols = x.out_col_ptrs;
+    a.keys = x.keys;
+    a.pool = x.dom_pool;
+    a.tile_counter = x.tile_counter;
+    a.scanned = x.scanned;
+    a.status = x.status;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    static int blocks[64] = {0};
+    if (blocks[dev] == 0) blocks[dev] = expand_grid_blocks(dev);
+    const int64_t need = (x.ntiles + kExpandWarps - 1) / kExpandWarps;
+    const int grid = (int)(need < blocks[dev] ? need : blocks[dev]);
+    const size_t smem = sizeof(WarpScratch) * kExpandWarps;
+    if (pass == Pass::Count)
+        k_expand<Pass::Count><<<grid, kExpandThreads, smem, st>>>(a);
+    else
+        k_expand<Pass::Support><<<grid, kExpandThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_domain_sizes(const DomDesc* dom, int32_t nact, const uint32_t* pool, uint32_t* sizes,
+                                cudaStream_t st)
+{
+    if (nact == 0) return cudaSuccess;
+    k_domain_sizes<<<nact * kMaxV, 256, 0, st>>>(dom, pool, sizes);
+    return cudaGetLastError();
+}
+
+}  // namespace gs

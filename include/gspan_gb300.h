@@ -1,0 +1,127 @@
+/*
+ * gspan_gb300 — C ABI of the GB300 frequent-subgraph miner.
+ *
+ * gSpan pattern growth over ONE undirected, vertex- and edge-labelled graph with
+ * MNI (minimum-image) support, computed by CUDA kernels on one GPU.  The ABI
+ * takes plain pointers and sizes; every call returns a status code and never
+ * throws.  Results (pattern, support) come back through a callback in the same
+ * order in which haozixu/gSpan prints them.
+ *
+ * Reference interfaces replaced (file:line in haozixu/gSpan):
+ *   gspan_graph_upload  <- CSRGraph + init_gpu_context      (graph.h:51-65, gspan.cu:97-127)
+ *   gspan_mine          <- void fsm(const CSRGraph&, int k, int min_support)
+ *                                                           (gspan.h:41, gspan.cu:1171-1199)
+ *   gspan_emit_fn       <- report()/print_dfs_code()        (gspan.cu:67-77)
+ *   gspan_is_canonical  <- is_canonical(const DFSCode&)     (gspan.cu:586-606)
+ *
+ * Threading: a context is used by one host thread at a time.  A context owns
+ * its CUDA stream and all device memory it allocates; graphs are owned by the
+ * context that uploaded them and must be freed before it is destroyed.
+ */
+#ifndef GSPAN_GB300_H_
+#define GSPAN_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gspan_status {
+    GSPAN_OK = 0,
+    GSPAN_ERR_INVALID = 1,   /* bad argument or malformed graph */
+    GSPAN_ERR_CUDA = 2,      /* a CUDA runtime call failed (message in gspan_last_error) */
+    GSPAN_ERR_NOMEM = 3,     /* device or host allocation failed, or over the memory budget */
+    GSPAN_ERR_LIMIT = 4,     /* beyond a documented size limit (pattern size, label count) */
+    GSPAN_ERR_DEVICE = 5,    /* a kernel reported an internal error through its status word */
+    GSPAN_ERR_ABORTED = 6,   /* the emit callback asked to stop */
+    GSPAN_ERR_NO_DEVICE = 7  /* no CUDA device is visible */
+} gspan_status;
+
+/* One directed CSR entry, layout-identical to the reference's `Edge`
+ * (graph.h:7-12): 12 bytes, from / to / label. */
+typedef struct gspan_edge {
+    int32_t from, to, label;
+} gspan_edge;
+
+/* One DFS-code edge, layout-identical to the reference's `PatternEdge`
+ * (graph.h:28-47).  Labels that the code does not fix are -1. */
+typedef struct gspan_pattern_edge {
+    int32_t from, to, from_label, edge_label, to_label;
+} gspan_pattern_edge;
+
+typedef struct gspan_opts {
+    int32_t device;              /* CUDA device ordinal (default 0) */
+    int32_t domain_mode;         /* 0 auto (bitmap or hashset per domain), 1 bitmaps only, 2 hashsets only */
+    double hash_threshold;       /* auto mode: a domain uses a hashset when 64 * max_size < |V| * hash_threshold.
+                                    0 selects the default (1.0) */
+    double mem_fraction;         /* share of free device memory the miner may hold (0 = 0.85) */
+    int32_t profile;             /* 1: time every kernel launch with CUDA events into gspan_stats */
+} gspan_opts;
+
+/* Run statistics.  Counts are exact and identical to those of the reference's
+ * CPU path on the same input (extension outputs of every extended pattern). */
+typedef struct gspan_stats {
+    uint64_t seeds;              /* level-1 embeddings (directed edges with from_label <= to_label) */
+    uint64_t extended;           /* child embeddings produced by extending frequent patterns */
+    uint64_t patterns;           /* reported (frequent, minimum-code) patterns */
+    uint64_t support_keys;       /* candidate patterns whose MNI support was counted */
+    uint64_t hash_domains;       /* of their vertex domains, how many used hashsets */
+    uint64_t scanned_entries;    /* adjacency entries read by the extension kernels */
+    uint64_t materialized_rows;  /* child embedding rows written to HBM */
+    uint64_t kernel_launches;    /* kernels of this library launched during gspan_mine */
+    int32_t levels;              /* deepest pattern size reached */
+    double mine_ms;              /* host wall time of gspan_mine */
+    /* profile == 1 only: per kernel family, CUDA-event time summed over launches */
+    double expand_ms;            /* extension kernels (count + support/materialise passes) */
+    uint64_t expand_launches;
+    double expand_bytes;         /* algorithmic bytes moved by those launches */
+    double seed_ms;
+    double domain_ms;            /* domain-size reductions */
+} gspan_stats;
+
+typedef struct gspan_ctx gspan_ctx;
+typedef struct gspan_graph gspan_graph;
+
+/* Receives one frequent pattern: `code[0..len)` and its MNI support.  Return 0
+ * to continue, non-zero to stop mining (gspan_mine then returns ABORTED). */
+typedef int (*gspan_emit_fn)(void* user, const gspan_pattern_edge* code, int32_t len, int32_t support);
+
+void gspan_opts_default(gspan_opts* opts);
+
+/* Creates a context on opts->device (NULL: defaults).  Fails with NO_DEVICE
+ * when no GPU is visible: there is no CPU fallback. */
+gspan_status gspan_ctx_create(const gspan_opts* opts, gspan_ctx** out);
+void gspan_ctx_destroy(gspan_ctx* ctx);
+
+/* Copies a host CSR graph in the reference's layout (graph.h:51-65: offsets[n+1],
+ * vlabels[n], edges[m], every undirected edge stored in both directions) into
+ * the device store.  The host arrays are not retained. */
+gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t nr_nodes, int32_t nr_edges,
+                                const int32_t* offsets, const int32_t* vlabels,
+                                const gspan_edge* edges, gspan_graph** out);
+gspan_status gspan_graph_free(gspan_ctx* ctx, gspan_graph* graph);
+
+/* Mines every frequent pattern with at most `k` edges whose MNI support is
+ * >= min_support, and emits them in the reference's pre-order.  k < 1 returns
+ * INVALID (the reference aborts on it); k > gspan_max_pattern_edges() returns
+ * LIMIT.  `stats` may be NULL. */
+gspan_status gspan_mine(gspan_ctx* ctx, const gspan_graph* graph, int32_t k, int32_t min_support,
+                        gspan_emit_fn emit, void* user, gspan_stats* stats);
+
+/* Host-only: whether `code` is a minimum DFS code by the reference's test
+ * (gspan.cu:586-606).  Writes 1 or 0 to *out. */
+gspan_status gspan_is_canonical(const gspan_pattern_edge* code, int32_t len, int32_t* out);
+
+const char* gspan_status_string(gspan_status s);
+/* Message of the last failure on this context (empty if none). */
+const char* gspan_last_error(const gspan_ctx* ctx);
+
+/* Largest supported pattern size in edges (k beyond it returns LIMIT). */
+int32_t gspan_max_pattern_edges(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSPAN_GB300_H_ */

@@ -1,0 +1,53 @@
+// Test infrastructure only: the CPU oracle for the mining path.
+//
+// A restatement of haozixu/gSpan's CPU algorithm (gspan.cu, graph.cc) in this
+// repository's own code.  It is the checker for the CUDA engine and the timed
+// CPU baseline; nothing in the product links or calls it.
+//
+// Parity pin: this port is validated line-by-line against the reference's own
+// sources compiled here (oracle/_ref/fsm, see ref_support_shim.h), and against
+// the golden outputs under tests/golden/ that the reference produced.
+#pragma once
+
+#include <cstdint>
+#include <functional>
+#include <vector>
+
+namespace port {
+
+struct Edge { int from, to, label; };            // graph.h:7-12
+
+struct Graph {                                   // graph.h:51-65 (CSRGraph)
+    int n = 0, m = 0;
+    std::vector<int> offsets, vlabels;
+    std::vector<Edge> edges;
+};
+
+struct PEdge {                                   // graph.h:28-47 (PatternEdge)
+    int from, to, fl, el, tl;
+    bool forward() const { return from < to; }
+    bool operator==(const PEdge& o) const {
+        return from == o.from && to == o.to && fl == o.fl && el == o.el && tl == o.tl;
+    }
+};
+using Code = std::vector<PEdge>;
+
+struct Stats {
+    uint64_t seeds = 0;          // level-1 embeddings
+    uint64_t extended = 0;       // child embeddings produced by extension
+    uint64_t patterns = 0;       // reported patterns
+    uint64_t support_calls = 0;  // canonical candidates whose support was counted
+};
+
+using ReportFn = std::function<void(const Code&, int support)>;
+
+// Runs the whole mining job; calls `report` in the reference's pre-order.
+void mine_all(const Graph& g, int k, int min_support, const ReportFn& report, Stats* stats);
+
+// The minimum-DFS-code test of gspan.cu:586-606 on its own (for unit tests).
+bool is_canonical(const Code& code);
+
+// Loads the reference's binary CSR file (graph.cc:178-200); false on a short read.
+bool load_bin(const char* path, Graph& g);
+
+}  // namespace port

@@ -1,0 +1,112 @@
+"""Parity of the CUDA miner with the reference, through the C ABI.
+
+Bit-exact: the pattern lines (codes, supports, order) must equal the
+reference's (golden fixtures made by the reference itself) or the CPU oracle
+port's, and the embedding counts must equal the oracle port's.
+"""
+import os
+import subprocess
+import tempfile
+
+import pytest
+
+from helpers import (ROOT, golden_cases, golden_graph, golden_lines, lines_of, random_graphs, run_port)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def miner():
+    from gspan_gb300 import Miner
+    m = Miner()
+    yield m
+    m.close()
+
+
+@pytest.mark.parametrize("case", golden_cases(), ids=lambda c: f"{c['name']}-s{c['min_support']}-k{c['k']}")
+def test_golden(miner, case):
+    g = golden_graph(case)
+    patterns, _ = miner.fsm(g, case["k"], case["min_support"])
+    assert lines_of(patterns) == golden_lines(case)
+
+
+@pytest.mark.parametrize("name,g,runs", random_graphs(), ids=lambda x: x if isinstance(x, str) else "")
+def test_random_vs_oracle(miner, name, g, runs):
+    dg = miner.upload(g)
+    try:
+        for sup, k in runs:
+            patterns, st = miner.mine(dg, k, sup)
+            ref, ref_st = run_port(g, sup, k, threads=4, with_stats=True)
+            assert lines_of(patterns) == ref, (name, sup, k)
+            assert st["seeds"] == ref_st["seeds"]
+            assert st["extended"] == ref_st["extended"]
+            assert st["patterns"] == ref_st["patterns"]
+    finally:
+        miner.free(dg)
+
+
+@pytest.mark.parametrize("mode,thr", [(1, 1.0), (2, 1.0), (0, 1e9), (0, 1e-9)])
+def test_domain_switch_same_supports(mode, thr):
+    """Bitmap and hashset domains give identical supports on both sides of the switch."""
+    from gspan_gb300 import Miner, datagen
+    g = datagen.chung_lu(3000, 9000, 2.1, 5, 1.0, 77, max_deg=150)
+    want = run_port(g, 40, 3, threads=4)
+    with Miner(domain_mode=mode, hash_threshold=thr) as m:
+        patterns, st = m.fsm(g, 3, 40)
+    assert lines_of(patterns) == want
+    if mode == 2 or thr > 1:
+        assert st["hash_domains"] > 0
+    if mode == 1 or thr < 1e-6:
+        assert st["hash_domains"] == 0
+
+
+def test_repeat_is_identical(miner):
+    from gspan_gb300 import datagen
+    g = datagen.er_3300(0)
+    dg = miner.upload(g)
+    try:
+        a, sa = miner.mine(dg, 3, 20)
+        b, sb = miner.mine(dg, 3, 20)
+    finally:
+        miner.free(dg)
+    assert a == b
+    assert sa["extended"] == sb["extended"]
+
+
+def test_errors(miner):
+    from gspan_gb300 import GspanError, datagen
+    g = datagen.er_3300(0)
+    dg = miner.upload(g)
+    try:
+        with pytest.raises(GspanError) as e:
+            miner.mine(dg, 0, 10)
+        assert e.value.status == 1
+        with pytest.raises(GspanError) as e:
+            miner.mine(dg, 16, 10)
+        assert e.value.status == 4
+    finally:
+        miner.free(dg)
+    bad = datagen.er_3300(0)
+    bad.edges = bad.edges.copy()
+    bad.edges[5, 0] += 1          # an entry whose `from` is not its vertex
+    with pytest.raises(GspanError) as e:
+        miner.upload(bad)
+    assert e.value.status == 1
+    bad2 = datagen.er_3300(0)
+    bad2.edges = bad2.edges.copy()
+    bad2.edges[7, 1] = 10 ** 6    # `to` out of range
+    with pytest.raises(GspanError):
+        miner.upload(bad2)
+
+
+def test_fsm_cli_matches_golden():
+    """The drop-in `fsm` program (graph.h loader + gspan.h fsm) prints the reference's lines."""
+    case = [c for c in golden_cases() if c["name"] == "er3300" and c["min_support"] == 20][0]
+    g = golden_graph(case)
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "g.bin")
+        g.save(path)
+        out = subprocess.run([os.path.join(ROOT, "gspan_gb300", "_lib", "fsm"), path, "20", "3"],
+                             capture_output=True, text=True, check=True).stdout.splitlines()
+    assert out[-1].startswith("load:")
+    assert out[:-1] == golden_lines(case)
