@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Mining benchmark: one JSON line on stdout (rank 0).
+
+A step is one complete mining job - every frequent pattern with at most k
+edges and its exact MNI support - over one seeded synthetic graph:
+
+  default workload  Chung-Lu power-law graph, 100,000 vertices, 1,080,000
+                    edges, exponent 2.1, expected-degree cap 1,400, 29 vertex
+                    labels Zipf(1.0), 1 edge label, seed 1; min support
+                    10,000; patterns up to 3 edges.
+
+value  = extended embeddings per second with the graph already resident in
+         HBM (child embeddings produced by extending frequent patterns; the
+         same count the reference's CPU path produces for this job).
+e2e    = the same metric through the C ABI from pinned host buffers: graph
+         upload (host->device, adjacency build), mining, results back to host.
+roofline = the extension kernel: algorithmic bytes / CUDA-event time, against
+         the measured HBM copy bandwidth.
+cpu_baseline = the CPU oracle port (the reference's algorithm, OpenMP on all
+         host cores) on a bounded sample of the same workload: the same graph
+         and threshold at 2 edges.
+
+--impl reference times that CPU implementation alone (rank 0; other ranks
+exit) and prints the same line with "impl": "reference".
+
+Multi-GPU (torchrun, N > 1): replicas only - every rank mines the same job on
+its own GPU; value = jobs' embeddings on all ranks / slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "mining time & embeddings/s, batched vs plain on 1 GB300 (exact patterns+MNI)"
+UNIT = "embeddings/s"
+
+
+def workloads():
+    from gspan_gb300 import datagen
+    return {
+        "chung_lu_100k": dict(
+            make=lambda: datagen.chung_lu_100k(1), min_support=10000, k=3, sample_k=2,
+            desc="Chung-Lu 100,000 V / 1,080,000 E, exponent 2.1, degree cap 1,400, 29 vertex labels Zipf(1.0), "
+                 "1 edge label, seed 1"),
+        # Smaller case of the same kernels for profiler captures: the same graph
+        # at a threshold that leaves one frequent 2-edge pattern to extend.
+        "chung_lu_100k_s15k": dict(
+            make=lambda: datagen.chung_lu_100k(1), min_support=15000, k=3, sample_k=2,
+            desc="Chung-Lu 100,000 V / 1,080,000 E (as chung_lu_100k), min support 15,000"),
+        "er_3300": dict(
+            make=lambda: datagen.er_3300(0), min_support=20, k=3, sample_k=3,
+            desc="Erdos-Renyi 3,300 V / 4,700 E, 6 uniform vertex labels, 1 edge label, seed 0"),
+    }
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_port(graph_path: str, min_support: int, k: int, cores: int) -> dict:
+    """One run of the CPU oracle port; returns its counts and fsm time."""
+    port = os.path.join(ROOT, "oracle", "_port", "fsm_port")
+    if not os.path.exists(port):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+    env = dict(os.environ, OMP_NUM_THREADS=str(cores), CUDA_VISIBLE_DEVICES="")
+    r = subprocess.run([port, graph_path, str(min_support), str(k), "--stats"], capture_output=True, text=True,
+                       check=True, env=env)
+    return json.loads(r.stderr.strip().splitlines()[-1])
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [p.strip() for p in line.split(",")]
+                    if len(parts) >= 9 and parts[1].isdigit():
+                        rows.append(parts)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [int(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": int(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace('.', '').isdigit())
+                if any(r[3].replace('.', '').isdigit() for r in rows) else None}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reference_arm(args, wl) -> None:
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    cores = host_cores()
+    g = wl["make"]()
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "g.bin")
+        g.save(path)
+        for _ in range(args.warmup):
+            run_port(path, wl["min_support"], wl["sample_k"], cores)
+        runs = [run_port(path, wl["min_support"], wl["sample_k"], cores) for _ in range(args.steps)]
+    ext = sum(r["extended"] for r in runs)
+    secs = sum(r["fsm_s"] for r in runs)
+    value = ext / secs if secs > 0 else 0.0
+    sample = (f"{wl['desc']}; min support {wl['min_support']}; patterns up to {wl['sample_k']} edges "
+              f"(bounded sample of the {wl['k']}-edge job); oracle port, OpenMP")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(runs), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "config": {"workload": args.workload, "description": wl["desc"], "min_support": wl["min_support"],
+                   "k": wl["sample_k"], "parallelism": "cpu"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "extended_per_step": runs[0]["extended"], "patterns": runs[0]["patterns"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def gpu_arm(args, wl) -> None:
+    import numpy as np
+    import torch
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from gspan_gb300 import Miner
+
+    g = wl["make"]()
+    k, sup = wl["k"], wl["min_support"]
+    dev = torch.device("cuda", local)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    # Pinned host copies of the graph for the end-to-end leg.
+    off_h = torch.from_numpy(np.ascontiguousarray(g.offsets, dtype=np.int32)).pin_memory()
+    vl_h = torch.from_numpy(np.ascontiguousarray(g.vlabels, dtype=np.int32)).pin_memory()
+    ed_h = torch.from_numpy(np.ascontiguousarray(g.edges, dtype=np.int32)).pin_memory()
+    h2d_graph = off_h.numel() * 4 + vl_h.numel() * 4 + ed_h.numel() * 4
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        with tempfile.TemporaryDirectory() as tmp:
+            path = os.path.join(tmp, "g.bin")
+            g.save(path)
+            cores = host_cores()
+            r = run_port(path, sup, wl["sample_k"], cores)
+        cpu = {"value": r["extended"] / r["fsm_s"], "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{wl['desc']}; min support {sup}; patterns up to {wl['sample_k']} edges "
+                         f"({r['extended']} extended embeddings in {r['fsm_s']:.3f} s); oracle port, OpenMP"}
+
+    with Miner(device=local, profile=True) as m:
+        dg = m.upload_arrays(off_h, vl_h, ed_h)
+        for _ in range(args.warmup):
+            patterns, st = m.mine(dg, k, sup)
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        step_ms, stats = [], []
+        barrier()
+        with ClockSampler(local) as clk:
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize(dev)
+                start.record()
+                patterns, st = m.mine(dg, k, sup)
+                end.record()
+                end.synchronize()
+                step_ms.append(start.elapsed_time(end))
+                stats.append(st)
+            barrier()
+            # End to end through the C ABI from pinned host memory.
+            e2e_ms, e2e_d2h = [], []
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize(dev)
+                start.record()
+                dg2 = m.upload_arrays(off_h, vl_h, ed_h)
+                pats2, st2 = m.mine(dg2, k, sup)
+                m.free(dg2)
+                end.record()
+                end.synchronize()
+                e2e_ms.append(start.elapsed_time(end))
+                e2e_d2h.append(st2["d2h_bytes"] + sum(20 * len(c) + 4 for c, _ in pats2))
+            barrier()
+        clocks = clk.summary()
+        m.free(dg)
+    total_ms = sum(step_ms)
+    e2e_total = sum(e2e_ms)
+    ext = sum(s["extended"] for s in stats)
+    if world > 1:
+        t = torch.tensor([total_ms, e2e_total], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms, e2e_total = float(t[0]), float(t[1])
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    value = world * ext / (total_ms / 1e3)
+    e2e_value = world * ext / (e2e_total / 1e3)
+    exp_ms = sum(s["expand_ms"] for s in stats)
+    exp_bytes = sum(s["expand_bytes"] for s in stats)
+    exp_launches = sum(s["expand_launches"] for s in stats)
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+        peaks = json.load(f)
+    peak = peaks.get("hbm_gbs") or 6800.0
+    achieved = exp_bytes / (exp_ms / 1e3) / 1e9 if exp_ms > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "expand_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(args.workload)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / len(step_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "config": {"workload": args.workload, "description": wl["desc"], "min_support": sup, "k": k,
+                   "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "engine": "plain (level-synchronous)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_total / len(e2e_ms),
+                "h2d_bytes_per_step": int(h2d_graph + stats[-1]["h2d_bytes"]),
+                "d2h_bytes_per_step": int(statistics.median(e2e_d2h))},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "kernel": "k_expand (count + support passes)", "launches_per_step": exp_launches / len(stats),
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "cpu_baseline": cpu,
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "clocks": clocks,
+        "extended_per_step": stats[-1]["extended"], "patterns": stats[-1]["patterns"],
+        "mining_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
+        "kernel_ms_per_step": {"expand": exp_ms / len(stats),
+                               "seed": sum(s["seed_ms"] for s in stats) / len(stats),
+                               "domain": sum(s["domain_ms"] for s in stats) / len(stats)},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", default="chung_lu_100k")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    wl = workloads()[args.workload]
+    if args.impl == "reference":
+        reference_arm(args, wl)
+    else:
+        gpu_arm(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -63,7 +63,8 @@ class Stats(ctypes.Structure):
                 ("scanned_entries", ctypes.c_uint64), ("materialized_rows", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint64), ("levels", ctypes.c_int32), ("mine_ms", ctypes.c_double),
                 ("expand_ms", ctypes.c_double), ("expand_launches", ctypes.c_uint64),
-                ("expand_bytes", ctypes.c_double), ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double)]
+                ("expand_bytes", ctypes.c_double), ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double),
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

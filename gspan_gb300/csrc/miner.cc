@@ -179,6 +179,14 @@ struct Run {
     cudaStream_t s;
     bool profile;
 
+    // Every host<->device copy of a mining run goes through here and is counted.
+    cudaError_t copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t strm)
+    {
+        if (kind == cudaMemcpyHostToDevice) st.h2d_bytes += bytes;
+        if (kind == cudaMemcpyDeviceToHost) st.d2h_bytes += bytes;
+        return cudaMemcpyAsync(dst, src, bytes, kind, strm);
+    }
+
     bool use_hash(uint64_t count) const
     {
         const int mode = ctx->opts.domain_mode;
@@ -228,17 +236,17 @@ struct Run {
         for (size_t i = 0; i < act.size(); ++i) act_h[act[i].key] = (int32_t)i;
 
         GS_CK(dalloc(&as.d_act, (size_t)nkeys, s), "alloc act");
-        GS_CK(cudaMemcpyAsync(as.d_act, act_h.data(), act_h.size() * 4, cudaMemcpyHostToDevice, s), "copy act");
+        GS_CK(copy(as.d_act, act_h.data(), act_h.size() * 4, cudaMemcpyHostToDevice, s), "copy act");
         if (as.nact > 0) {
             GS_CK(dalloc(&as.pool, bitmap_words + hash_words, s), "alloc domains");
             if (bitmap_words) GS_CK(cudaMemsetAsync(as.pool, 0, bitmap_words * 4, s), "clear bitmaps");
             if (hash_words)
                 GS_CK(cudaMemsetAsync(as.pool + bitmap_words, 0xFF, hash_words * 4, s), "clear hashsets");
             GS_CK(dalloc(&as.d_dom, act.size(), s), "alloc dom");
-            GS_CK(cudaMemcpyAsync(as.d_dom, as.dom.data(), act.size() * sizeof(DomDesc), cudaMemcpyHostToDevice, s),
+            GS_CK(copy(as.d_dom, as.dom.data(), act.size() * sizeof(DomDesc), cudaMemcpyHostToDevice, s),
                   "copy dom");
             GS_CK(dalloc(&as.d_mat, act.size(), s), "alloc mat");
-            GS_CK(cudaMemcpyAsync(as.d_mat, as.mat.data(), act.size() * sizeof(long long), cudaMemcpyHostToDevice, s),
+            GS_CK(copy(as.d_mat, as.mat.data(), act.size() * sizeof(long long), cudaMemcpyHostToDevice, s),
                   "copy mat");
             GS_CK(dalloc(&as.d_cursor, act.size(), s), "alloc cursor");
             GS_CK(cudaMemsetAsync(as.d_cursor, 0, act.size() * 8, s), "clear cursor");
@@ -249,7 +257,7 @@ struct Run {
             out.cols.assign(out_cols, nullptr);
             for (int c = 0; c < out_cols; ++c) GS_CK(dalloc(&out.cols[c], (size_t)out_rows, s), "alloc level table");
             GS_CK(dalloc(&out.d_cols, (size_t)out_cols, s), "alloc column table");
-            GS_CK(cudaMemcpyAsync(out.d_cols, out.cols.data(), out_cols * sizeof(int32_t*), cudaMemcpyHostToDevice, s),
+            GS_CK(copy(out.d_cols, out.cols.data(), out_cols * sizeof(int32_t*), cudaMemcpyHostToDevice, s),
                   "copy column table");
             st.materialized_rows += (uint64_t)out_rows;
         }
@@ -270,9 +278,9 @@ struct Run {
         if (profile) cudaEventRecord(ctx->ev_d, s);
         ++st.kernel_launches;
         std::vector<uint32_t> h((size_t)as.nact * kMaxV);
-        GS_CK(cudaMemcpyAsync(h.data(), d_sizes, h.size() * 4, cudaMemcpyDeviceToHost, s), "read sizes");
+        GS_CK(copy(h.data(), d_sizes, h.size() * 4, cudaMemcpyDeviceToHost, s), "read sizes");
         uint32_t status = 0;
-        GS_CK(cudaMemcpyAsync(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
+        GS_CK(copy(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
         GS_CK(cudaStreamSynchronize(s), "domain sizes");
         dfree(d_sizes, s);
         if (profile) {
@@ -305,7 +313,7 @@ struct Run {
         GS_CK(launch_seed_count(g, d_counts, s), "seed count launch");
         ++st.kernel_launches;
         std::vector<unsigned long long> counts((size_t)nkeys);
-        GS_CK(cudaMemcpyAsync(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read seed counts");
+        GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read seed counts");
         GS_CK(cudaStreamSynchronize(s), "seed count");
         std::vector<Active> act;
         for (int64_t key = 0; key < nkeys; ++key) {
@@ -404,7 +412,7 @@ struct Run {
         ParentMeta* d_meta = nullptr;
         unsigned long long* d_counts = nullptr;
         GS_CK(dalloc(&d_meta, meta.size(), s), "alloc parents");
-        GS_CK(cudaMemcpyAsync(d_meta, meta.data(), meta.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s),
+        GS_CK(copy(d_meta, meta.data(), meta.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s),
               "copy parents");
         GS_CK(dalloc(&d_counts, (size_t)nkeys, s), "alloc counts");
         GS_CK(cudaMemsetAsync(d_counts, 0, nkeys * 8, s), "clear counts");
@@ -429,8 +437,8 @@ struct Run {
         ++st.kernel_launches;
         std::vector<unsigned long long> counts((size_t)nkeys);
         unsigned long long ctr[2] = {0, 0};
-        GS_CK(cudaMemcpyAsync(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read counts");
-        GS_CK(cudaMemcpyAsync(ctr, ctx->d_counters, 16, cudaMemcpyDeviceToHost, s), "read counters");
+        GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read counts");
+        GS_CK(copy(ctr, ctx->d_counters, 16, cudaMemcpyDeviceToHost, s), "read counters");
         GS_CK(cudaStreamSynchronize(s), "count pass");
         if (profile) {
             float ms = 0;

@@ -78,6 +78,8 @@ typedef struct gspan_stats {
     double expand_bytes;         /* algorithmic bytes moved by those launches */
     double seed_ms;
     double domain_ms;            /* domain-size reductions */
+    uint64_t h2d_bytes;          /* host->device bytes copied by gspan_mine */
+    uint64_t d2h_bytes;          /* device->host bytes copied by gspan_mine */
 } gspan_stats;
 
 typedef struct gspan_ctx gspan_ctx;
