@@ -255,9 +255,16 @@ def gpu_arm(args, wl) -> None:
         return
     value = world * ext / (total_ms / 1e3)
     e2e_value = world * ext / (e2e_total / 1e3)
-    exp_ms = sum(s["expand_ms"] for s in stats)
-    exp_bytes = sum(s["expand_bytes"] for s in stats)
-    exp_launches = sum(s["expand_launches"] for s in stats)
+    # Dominant kernel family by CUDA-event time over the timed steps.
+    fams = {"k_mask_rows (mask path row pass)": ("rows_ms", "rows_bytes", "rows_launches"),
+            "k_expand Count/Support (per-candidate path)": ("expand_ms", "expand_bytes", "expand_launches"),
+            "k_mask_sweep (mask path adjacency sweep)": ("sweep_ms", "sweep_bytes", "rows_launches"),
+            "k_expand Materialize (child rows)": ("materialize_ms", "materialize_bytes", "materialize_launches")}
+    fam_ms = {name: sum(s[f[0]] for s in stats) for name, f in fams.items()}
+    dom = max(fam_ms, key=fam_ms.get)
+    exp_ms = fam_ms[dom]
+    exp_bytes = sum(s[fams[dom][1]] for s in stats)
+    exp_launches = sum(s[fams[dom][2]] for s in stats)
     with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
         peaks = json.load(f)
     peak = peaks.get("hbm_gbs") or 6800.0
@@ -279,16 +286,17 @@ def gpu_arm(args, wl) -> None:
                 "d2h_bytes_per_step": int(statistics.median(e2e_d2h))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "kernel": "k_expand (count + support passes)", "launches_per_step": exp_launches / len(stats),
+                     "kernel": dom, "launches_per_step": exp_launches / len(stats),
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "cpu_baseline": cpu,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "clocks": clocks,
         "extended_per_step": stats[-1]["extended"], "patterns": stats[-1]["patterns"],
         "mining_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
-        "kernel_ms_per_step": {"expand": exp_ms / len(stats),
+        "kernel_ms_per_step": {**{name: ms / len(stats) for name, ms in fam_ms.items()},
                                "seed": sum(s["seed_ms"] for s in stats) / len(stats),
-                               "domain": sum(s["domain_ms"] for s in stats) / len(stats)},
+                               "domain sizes": sum(s["domain_ms"] for s in stats) / len(stats)},
+        "paths": {"mask_parents": stats[-1]["mask_parents"], "candidate_parents": stats[-1]["candidate_parents"]},
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -54,7 +54,7 @@ class GspanError(RuntimeError):
 class Opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("domain_mode", ctypes.c_int32),
                 ("hash_threshold", ctypes.c_double), ("mem_fraction", ctypes.c_double),
-                ("profile", ctypes.c_int32)]
+                ("profile", ctypes.c_int32), ("path", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -62,9 +62,15 @@ class Stats(ctypes.Structure):
                 ("support_keys", ctypes.c_uint64), ("hash_domains", ctypes.c_uint64),
                 ("scanned_entries", ctypes.c_uint64), ("materialized_rows", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint64), ("levels", ctypes.c_int32), ("mine_ms", ctypes.c_double),
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("mask_parents", ctypes.c_uint64), ("candidate_parents", ctypes.c_uint64),
                 ("expand_ms", ctypes.c_double), ("expand_launches", ctypes.c_uint64),
-                ("expand_bytes", ctypes.c_double), ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double),
-                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("expand_bytes", ctypes.c_double),
+                ("rows_ms", ctypes.c_double), ("rows_launches", ctypes.c_uint64), ("rows_bytes", ctypes.c_double),
+                ("sweep_ms", ctypes.c_double), ("sweep_bytes", ctypes.c_double),
+                ("materialize_ms", ctypes.c_double), ("materialize_launches", ctypes.c_uint64),
+                ("materialize_bytes", ctypes.c_double),
+                ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -140,7 +146,7 @@ class Miner:
     """One mining context on one GPU (a CUDA stream and the device memory it owns)."""
 
     def __init__(self, device: int = 0, domain_mode: int = 0, hash_threshold: float = 1.0,
-                 profile: bool = False, mem_fraction: float = 0.85):
+                 profile: bool = False, mem_fraction: float = 0.85, path: int = 0):
         opts = Opts()
         _lib.gspan_opts_default(ctypes.byref(opts))
         opts.device = device
@@ -148,6 +154,7 @@ class Miner:
         opts.hash_threshold = hash_threshold
         opts.profile = 1 if profile else 0
         opts.mem_fraction = mem_fraction
+        opts.path = path
         self._ctx = ctypes.c_void_p()
         rc = _lib.gspan_ctx_create(ctypes.byref(opts), ctypes.byref(self._ctx))
         if rc != GSPAN_OK:

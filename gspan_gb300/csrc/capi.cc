@@ -70,6 +70,8 @@ void free_graph(gspan_graph* gr, cudaStream_t st)
     if (g.adj) cudaFreeAsync(g.adj, st);
     if (g.src) cudaFreeAsync(g.src, st);
     if (g.vrank) cudaFreeAsync(g.vrank, st);
+    if (g.segmask) cudaFreeAsync(g.segmask, st);
+    g.segmask = nullptr;
     g.offsets = nullptr;
     g.adj = nullptr;
     g.src = nullptr;
@@ -89,6 +91,7 @@ void gspan_opts_default(gspan_opts* o)
     o->hash_threshold = 1.0;
     o->mem_fraction = 0.85;
     o->profile = 0;
+    o->path = 0;
 }
 
 const char* gspan_status_string(gspan_status s)
@@ -144,7 +147,7 @@ gspan_status gspan_ctx_create(const gspan_opts* opts, gspan_ctx** out)
     for (cudaEvent_t* ev : {&ctx->ev_a, &ctx->ev_b, &ctx->ev_c, &ctx->ev_d})
         if ((e = cudaEventCreate(ev)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&ctx->d_status, 4)) != cudaSuccess) return bail(e);
-    if ((e = cudaMalloc(&ctx->d_counters, 16)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&ctx->d_counters, 32)) != cudaSuccess) return bail(e);
     // Keep freed stream-ordered blocks cached in this process, so the many
     // per-level buffers of repeated mining runs do not go back to the driver.
     cudaMemPool_t pool;
@@ -238,6 +241,16 @@ gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t n, int32_t m, const int3
     UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
     UP_CK(gs::launch_build_adjacency(g.offsets, d_edges, g.vrank, d_elabels, g.nel, g, d_tmp, ctx->d_status, s),
           "build adjacency launch");
+    // Per-vertex masks of the (edge label, to label) segments present, for the
+    // mask extension path; only when the tuple space fits the mask width.
+    {
+        const int64_t K = (int64_t)g.nel * g.nvl;
+        if (n > 0 && K > 0 && K <= 32 * gs::kMaxMaskWords) {
+            g.segw = (int32_t)((K + 31) / 32);
+            UP_CK(cudaMallocAsync(&g.segmask, (size_t)n * g.segw * 4, s), "alloc segment masks");
+            UP_CK(gs::launch_segmask(g, s), "segment mask launch");
+        }
+    }
     uint32_t status = 0;
     UP_CK(cudaMemcpyAsync(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
     cleanup();

@@ -45,8 +45,16 @@ struct DevGraph {
     uint64_t* adj = nullptr;    // [m] packed entries, sorted per vertex
     int32_t* src = nullptr;     // [m] owning vertex of each entry
     int32_t* vrank = nullptr;   // [n] vertex label rank
+    // Per vertex, `segw` words with bit (el * nvl + tl) set when the vertex has
+    // a neighbour entry with that (edge label, to label).  Built when the key
+    // space nel * nvl fits kMaxMaskWords words, else null (segw = 0).
+    uint32_t* segmask = nullptr;
+    int32_t segw = 0;
     std::vector<int32_t> vlabel_of_rank, elabel_of_rank;
 };
+
+// Widest per-vertex key mask the mask kernels handle (x 32 keys).
+constexpr int kMaxMaskWords = 4;
 
 // Where a domain (set of graph vertices that one pattern vertex maps to)
 // lives: `nvc` consecutive tables of `cap` 32-bit words starting at `off` in
@@ -89,6 +97,25 @@ struct ParentMeta {
     int8_t e_from[kMaxE];       // parent code edges, for the has_edge test
     int8_t e_to[kMaxE];
     int16_t e_el[kMaxE];
+    // Mask path (see k_mask_rows): offsets of this parent's dense arrays.
+    int32_t bw;                 // words per backward-key mask
+    int64_t sweep_begin;        // first (source, vertex) task of this parent in the sweep
+    int64_t r_off;              // R: nsrc x n row counters
+    int64_t h_off;              // H: nsrc x m entry counters
+    int64_t m_off;              // M: nsrc x (nv+1) x n x segw words
+    int64_t b_off;              // MB: nv x n x bw words
+    uint32_t range[kMaxV][kMaxMaskWords];   // per source: keys inside its valid range
+};
+
+// One key-mask matrix whose column popcounts are domain sizes: `n` vertices x
+// `width` words at `base`; column kc adds to sizes[out + kc * stride].
+struct MaskMatrix {
+    int64_t base;
+    int64_t out;
+    int32_t width;
+    int32_t nbits;
+    int32_t stride;
+    int32_t in_mb;               // 1: offset into MB (backward keys), 0: into M
 };
 
 // Per-level key space arrays on the device.
@@ -100,7 +127,7 @@ struct LevelKeys {
     unsigned long long* cursor = nullptr;   // [nact]
 };
 
-enum class Pass : int { Count = 0, Support = 1 };
+enum class Pass : int { Count = 0, Support = 1, Materialize = 2 };
 
 struct ExpandArgs {
     const DevGraph* g;                 // host copy; device pointers inside are used
@@ -130,5 +157,28 @@ cudaError_t launch_domain_sizes(const DomDesc* dom, int32_t nact, const uint32_t
                                 uint32_t* sizes /* [nact * kMaxV] */, cudaStream_t st);
 
 int expand_grid_blocks(int device);
+
+// Mask path.
+struct MaskArgs {
+    const DevGraph* g;
+    const ParentMeta* parents;   // device, mask-path parents only
+    int32_t nparents;
+    int64_t ntiles;
+    int64_t nsweep;              // total (parent, source, vertex) sweep tasks
+    int32_t* const* in_col_ptrs;
+    unsigned long long* counts;  // level key space
+    uint32_t* R;
+    uint32_t* H;
+    uint32_t* M;
+    uint32_t* MB;
+    unsigned long long* tile_counter;
+    unsigned long long* scanned;  // adjacency entries read by the sweep
+    uint32_t* status;
+};
+cudaError_t launch_segmask(DevGraph& g, cudaStream_t st);
+cudaError_t launch_mask_rows(const MaskArgs& a, cudaStream_t st);
+cudaError_t launch_mask_sweep(const MaskArgs& a, cudaStream_t st);
+cudaError_t launch_mask_sizes(const MaskMatrix* mats, int32_t nmats, const uint32_t* M, const uint32_t* MB,
+                              int32_t n, uint32_t* sizes, cudaStream_t st);
 
 }  // namespace gs

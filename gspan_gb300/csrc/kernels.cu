@@ -20,6 +20,8 @@
 //  * domain_sizes    : popcount / occupied-slot count of every domain.
 #include "engine.h"
 
+#include <algorithm>
+
 namespace gs {
 namespace {
 
@@ -207,9 +209,14 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
             unsigned long long at = 0;
             if (lane == leader) at = atomicAdd(keys.cursor + a, (unsigned long long)__popc(peers));
             at = __shfl_sync(mm, at, leader);
-            const long long row = keys.mat_off[a] + (long long)at + __popc(peers & lanemask_lt());
-            col0[row] = (int32_t)u;
-            col1[row] = (int32_t)w;
+            const unsigned long long slot = at + __popc(peers & lanemask_lt());
+            if (slot < keys.counts[key]) {
+                const long long row = keys.mat_off[a] + (long long)slot;
+                col0[row] = (int32_t)u;
+                col1[row] = (int32_t)w;
+            } else {
+                atomicOr(status, kErrCursor);
+            }
         }
     }
 }
@@ -293,7 +300,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
         W.pre[lane] = incl - work;
         const int32_t total = __shfl_sync(kFull, incl, 31);
         __syncwarp();
-        if (kPass == Pass::Count && lane == 0 && total > 0)
+        if (kPass != Pass::Support && lane == 0 && total > 0)
             atomicAdd(a.scanned, (unsigned long long)total);
 
         // Backward candidates: at most one per (row, rightmost-path target).
@@ -333,12 +340,11 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
             } else {
                 const int32_t ai = ok ? a.keys.act[key] : -1;
                 const bool sup = ai >= 0;
-                DomDesc d{};
-                if (sup) {
-                    d = a.keys.dom[ai];
+                if (kPass == Pass::Support && sup) {
+                    const DomDesc d = a.keys.dom[ai];
                     for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)W.img[lane][p], a.status);
                 }
-                const bool mat = sup && a.keys.mat_off[ai] >= 0;
+                const bool mat = kPass == Pass::Materialize && sup;
                 const unsigned mm = __ballot_sync(kFull, mat);
                 if (mat) {
                     const unsigned peers = __match_any_sync(mm, ai);
@@ -346,8 +352,13 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                     unsigned long long at = 0;
                     if (lane == leader) at = atomicAdd(a.keys.cursor + ai, (unsigned long long)__popc(peers));
                     at = __shfl_sync(mm, at, leader);
-                    const long long r = a.keys.mat_off[ai] + (long long)at + __popc(peers & lanemask_lt());
-                    for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[lane][p];
+                    const unsigned long long slot = at + __popc(peers & lanemask_lt());
+                    if (slot < a.keys.counts[key]) {
+                        const long long r = a.keys.mat_off[ai] + (long long)slot;
+                        for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[lane][p];
+                    } else {
+                        atomicOr(a.status, kErrCursor);   // more candidates than counted: never write past the range
+                    }
                 }
             }
         }
@@ -389,17 +400,18 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
             } else {
                 const int32_t ai = ok ? a.keys.act[key] : -1;
                 const bool sup = ai >= 0;
-                const unsigned sm = __ballot_sync(kFull, sup);
-                DomDesc d{};
-                if (sup) {
-                    d = a.keys.dom[ai];
-                    dom_insert(a.pool, d, nv, to, a.status);
-                    // The parent row's images go in once per (row, child tuple) in this chunk.
-                    const unsigned peers = __match_any_sync(sm, ((unsigned long long)owner << 32) | (unsigned)ai);
-                    if (lane == __ffs(peers) - 1)
-                        for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)W.img[owner][p], a.status);
+                if (kPass == Pass::Support) {
+                    const unsigned sm = __ballot_sync(kFull, sup);
+                    if (sup) {
+                        const DomDesc d = a.keys.dom[ai];
+                        dom_insert(a.pool, d, nv, to, a.status);
+                        // The parent row's images go in once per (row, child tuple) in this chunk.
+                        const unsigned peers = __match_any_sync(sm, ((unsigned long long)owner << 32) | (unsigned)ai);
+                        if (lane == __ffs(peers) - 1)
+                            for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)W.img[owner][p], a.status);
+                    }
                 }
-                const bool mat = sup && a.keys.mat_off[ai] >= 0;
+                const bool mat = kPass == Pass::Materialize && sup;
                 const unsigned mm = __ballot_sync(kFull, mat);
                 if (mat) {
                     const unsigned peers = __match_any_sync(mm, ai);
@@ -407,13 +419,319 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                     unsigned long long at = 0;
                     if (lane == leader) at = atomicAdd(a.keys.cursor + ai, (unsigned long long)__popc(peers));
                     at = __shfl_sync(mm, at, leader);
-                    const long long r = a.keys.mat_off[ai] + (long long)at + __popc(peers & lanemask_lt());
-                    for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[owner][p];
-                    a.out_cols[nv][r] = (int32_t)to;
+                    const unsigned long long slot = at + __popc(peers & lanemask_lt());
+                    if (slot < a.keys.counts[key]) {
+                        const long long r = a.keys.mat_off[ai] + (long long)slot;
+                        for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[owner][p];
+                        a.out_cols[nv][r] = (int32_t)to;
+                    } else {
+                        atomicOr(a.status, kErrCursor);
+                    }
                 }
             }
         }
         __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mask path: counts and MNI domains of every child tuple without visiting
+// candidates one by one.
+//
+// For parent pattern P, source s (a rightmost-path vertex) and row r, let u_r be
+// the row's image of the source and seg(u, c) the adjacency entries of u with
+// (edge label, to label) = c.  The reference emits one child embedding per
+// entry e of seg(u_r, c) whose `to` is not an image of r (gspan.cu:447-483).
+// With
+//   R[u] = rows whose source image is u,
+//   H[e] = rows whose source image owns entry e and that have to(e) as an image,
+// the child count of tuple (s, c) is sum over entries e of seg(u, c) of
+// R[u] - H[e], and the new vertex's domain is {to(e) : R[u] > H[e]}.  An old
+// vertex p's domain for (s, c) is {img_r(p) : row r has an entry of
+// seg(u_r, c) outside its images}; the row pass ORs the set of such c (a
+// bitmask over the tuple space) into M[p][img_r(p)], so a domain size is the
+// popcount of one bit column of M.  All of it is exact.
+
+constexpr int kMaskWarps = 8;
+
+struct MaskDev {
+    const int32_t* offsets;
+    const uint64_t* adj;
+    const uint32_t* segmask;
+    int32_t n, m, nvl, nel, mw;
+    const ParentMeta* parents;
+    int32_t nparents;
+    int64_t ntiles;
+    int64_t nsweep;
+    int32_t* const* in_cols;
+    unsigned long long* counts;
+    uint32_t* R;
+    uint32_t* H;
+    uint32_t* M;
+    uint32_t* MB;
+    unsigned long long* tile_counter;
+    unsigned long long* scanned;
+    uint32_t* status;
+};
+
+__device__ __forceinline__ void or_words(uint32_t* p, uint32_t bits)
+{
+    if (bits && (__ldcg(p) & bits) != bits) atomicOr(p, bits);
+}
+
+__global__ void k_segmask(int32_t n, int32_t nvl, int32_t segw, const int32_t* __restrict__ offsets,
+                          const uint64_t* __restrict__ adj, uint32_t* __restrict__ segmask)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = warp; v < n; v += nwarps) {
+        uint32_t w[kMaxMaskWords] = {0, 0, 0, 0};
+        for (int32_t j = offsets[v] + lane; j < offsets[v + 1]; j += 32) {
+            const uint64_t ent = adj[j];
+            const uint32_t kc = entry_el(ent) * (uint32_t)nvl + entry_tl(ent);
+#pragma unroll
+            for (int i = 0; i < kMaxMaskWords; ++i) w[i] |= (uint32_t)(i == (int)(kc >> 5)) << (kc & 31u);
+        }
+#pragma unroll
+        for (int i = 0; i < kMaxMaskWords; ++i) {
+            const uint32_t r = __reduce_or_sync(kFull, w[i]);
+            if (lane == 0 && i < segw) segmask[v * segw + i] = r;
+        }
+    }
+}
+
+__device__ __forceinline__ int32_t find_parent_tile(const ParentMeta* parents, int32_t np, long long tile)
+{
+    int32_t lo = 0, hi = np - 1;
+    while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if (parents[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Row pass: lane per row.  Updates R, H and M for every source, and counts and
+// MB masks for backward tuples (at most one per row and rightmost-path target).
+__global__ void __launch_bounds__(kMaskWarps * 32) k_mask_rows(MaskDev a)
+{
+    __shared__ int32_t img_s[kMaskWarps][32][kMaxV + 1];
+    int32_t (*img_all)[kMaxV + 1] = img_s[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    int32_t* img = img_all[lane];
+    const int32_t K = a.nel * a.nvl;
+    const int mw = a.mw;
+
+    for (;;) {
+        long long tile = 0;
+        if (lane == 0) tile = (long long)atomicAdd(a.tile_counter, 1ull);
+        tile = __shfl_sync(kFull, tile, 0);
+        if (tile >= a.ntiles) break;
+        const ParentMeta& P = a.parents[find_parent_tile(a.parents, a.nparents, tile)];
+        const int nv = P.nv, nsrc = P.nsrc;
+        const int min_label = P.min_label;
+        const int64_t row = P.row_begin + (tile - P.tile_begin) * 32 + lane;
+        const bool live = row < P.row_end;
+        for (int p = 0; p < nv; ++p) img[p] = live ? __ldcs(a.in_cols[p] + row) : -1;
+
+        for (int s = 0; s < nsrc; ++s) {
+            const int32_t u = live ? img[P.src_v[s]] : -1;
+            const unsigned lm = __ballot_sync(kFull, live);
+            if (live) {
+                const unsigned peers = __match_any_sync(lm, u);
+                if (lane == __ffs(peers) - 1) atomicAdd(a.R + P.r_off + (int64_t)s * a.n + u, (uint32_t)__popc(peers));
+            }
+            if (!live) continue;
+            const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
+            const uint64_t lo = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
+                                       : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
+            uint32_t* Hs = a.H + P.h_off + (int64_t)s * a.m;
+            uint32_t ex[kMaxMaskWords] = {0, 0, 0, 0};
+            for (int el = 0; el < a.nel; ++el) {
+                for (int i = 0; i < nv; ++i) {
+                    const int t = P.vlab[i];
+                    const uint64_t seg0 = pack_entry((uint32_t)el, (uint32_t)t, 0);
+                    if (t < min_label || seg0 < lo) continue;
+                    bool lead = true;   // first pattern vertex of this label handles the label group
+                    for (int q = 0; q < i; ++q) lead &= P.vlab[q] != t;
+                    if (!lead) continue;
+                    int32_t hits = 0, minlb = e, maxub = b;
+                    for (int j = i; j < nv; ++j) {
+                        if (P.vlab[j] != t) continue;
+                        const int32_t x = img[j];
+                        bool dup = false;
+                        for (int q = i; q < j; ++q) dup |= img[q] == x;
+                        if (dup) continue;
+                        const uint64_t key = seg0 | (uint32_t)x;
+                        const int32_t lb = lower_bound_entry(a.adj, b, e, key);
+                        int32_t ub = lb;
+                        while (ub < e && __ldg(a.adj + ub) == key) {
+                            atomicAdd(Hs + ub, 1u);
+                            ++ub;
+                        }
+                        if (ub > lb) {
+                            hits += ub - lb;
+                            minlb = min(minlb, lb);
+                            maxub = max(maxub, ub);
+                        }
+                    }
+                    if (hits > 0) {
+                        // The row has no child in this segment when its images fill all of it.
+                        const uint32_t segk = (uint32_t)(seg0 >> 32);
+                        const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
+                        const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
+                        if (first && last && maxub - minlb == hits) {
+                            const uint32_t kc = (uint32_t)(el * a.nvl + t);
+#pragma unroll
+                            for (int w = 0; w < kMaxMaskWords; ++w)
+                                ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
+                        }
+                    }
+                }
+            }
+            uint32_t mk[kMaxMaskWords];
+#pragma unroll
+            for (int w = 0; w < kMaxMaskWords; ++w)
+                mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
+            for (int p = 0; p < nv; ++p) {
+                uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * a.n + img[p]) * mw;
+#pragma unroll
+                for (int w = 0; w < kMaxMaskWords; ++w)
+                    if (w < mw) or_words(rowm + w, mk[w]);
+            }
+        }
+
+        for (int t = 0; t < P.nback; ++t) {
+            bool ok = false;
+            int32_t bel = 0;
+            if (live) {
+                const int bv = P.back_v[t];
+                const int32_t x = img[bv];
+                const int32_t un = img[P.vn];
+                const uint32_t tlx = (uint32_t)P.vlab[bv];
+                const int32_t b = __ldg(a.offsets + un), e = __ldg(a.offsets + un + 1);
+                for (int32_t el = P.back_eq[t] ? P.back_el[t] : P.back_el[t] + 1; el < a.nel && !ok; ++el) {
+                    const uint64_t want = pack_entry((uint32_t)el, tlx, (uint32_t)x);
+                    const int32_t pos = lower_bound_entry(a.adj, b, e, want);
+                    if (pos < e && __ldg(a.adj + pos) == want) {
+                        bool used = false;
+                        for (int j = 0; j < P.nedge; ++j) {
+                            if (P.e_el[j] != el) continue;
+                            const int32_t f = img[P.e_from[j]], g2 = img[P.e_to[j]];
+                            if ((f == un && g2 == x) || (g2 == un && f == x)) used = true;
+                        }
+                        if (!used) {
+                            ok = true;
+                            bel = el;
+                        }
+                    }
+                }
+            }
+            const int32_t bk = t * a.nel + bel;
+            const int32_t key = P.key_base + nsrc * K + bk;
+            const unsigned mask = __ballot_sync(kFull, ok);
+            if (ok) {
+                const unsigned peers = __match_any_sync(mask, key);
+                if (lane == __ffs(peers) - 1) atomicAdd(a.counts + key, (unsigned long long)__popc(peers));
+                for (int p = 0; p < nv; ++p)
+                    or_words(a.MB + P.b_off + ((int64_t)p * a.n + img[p]) * P.bw + (bk >> 5), 1u << (bk & 31));
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Sweep: warp per (parent, source, vertex u with R[u] > 0) over u's entries in
+// the source's range: child counts by tuple and the new vertex's domain masks.
+__global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int32_t K = a.nel * a.nvl;
+    const int mw = a.mw;
+    unsigned long long scanned = 0;
+    for (int64_t task = warp; task < a.nsweep; task += nwarps) {
+        int32_t lo = 0, hi = a.nparents - 1;
+        while (lo < hi) {
+            const int32_t mid = (lo + hi + 1) >> 1;
+            if (a.parents[mid].sweep_begin <= task) lo = mid; else hi = mid - 1;
+        }
+        const ParentMeta& P = a.parents[lo];
+        const int64_t local = task - P.sweep_begin;
+        const int s = (int)(local / a.n);
+        const int32_t u = (int32_t)(local % a.n);
+        const uint32_t r = __ldg(a.R + P.r_off + (int64_t)s * a.n + u);
+        if (r == 0) continue;
+        const int min_label = P.min_label;
+        const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
+        const uint64_t lo_key = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
+                                       : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
+        const int32_t st = lower_bound_entry(a.adj, b, e, lo_key);
+        const uint32_t* Hs = a.H + P.h_off + (int64_t)s * a.m;
+        uint32_t* NM = a.M + P.m_off + ((int64_t)s * (P.nv + 1) + P.nv) * a.n * mw;
+        unsigned long long* cnt = a.counts + P.key_base + (int64_t)s * K;
+        scanned += (unsigned long long)(e - st);
+        for (int32_t base = st; base < e; base += 32) {
+            const int32_t i = base + lane;
+            bool ok = false;
+            int32_t kc = 0;
+            uint32_t diff = 0, to = 0;
+            if (i < e) {
+                const uint64_t ent = __ldg(a.adj + i);
+                const int32_t tl = (int32_t)entry_tl(ent);
+                ok = tl >= min_label;
+                kc = (int32_t)entry_el(ent) * a.nvl + tl;
+                to = entry_to(ent);
+                diff = r - __ldg(Hs + i);
+            }
+            // Entries are sorted by tuple, so equal tuples sit in adjacent lanes.
+            const int32_t segk = ok ? kc : (int32_t)(0x40000000 + lane);
+            unsigned long long v = ok ? diff : 0ull;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned long long uv = __shfl_up_sync(kFull, v, d);
+                const int32_t uk = __shfl_up_sync(kFull, segk, d);
+                if (lane >= d && uk == segk) v += uv;
+            }
+            const int32_t nk = __shfl_down_sync(kFull, segk, 1);
+            if (ok && (lane == 31 || nk != segk) && v) atomicAdd(cnt + kc, v);
+            if (ok && diff > 0) or_words(NM + (int64_t)to * mw + (kc >> 5), 1u << (kc & 31));
+        }
+    }
+    scanned += __shfl_xor_sync(kFull, scanned, 16);
+    if (lane == 0 && scanned) atomicAdd(a.scanned, scanned);
+}
+
+// Column popcounts of key-mask matrices: block row y = matrix, x-blocks split
+// the vertices; lane b of a warp accumulates bit b of each word.
+__global__ void __launch_bounds__(256) k_mask_sizes(const MaskMatrix* __restrict__ mats, const uint32_t* __restrict__ M,
+                                                    const uint32_t* __restrict__ MB, int32_t n,
+                                                    uint32_t* __restrict__ sizes)
+{
+    const MaskMatrix mm = mats[blockIdx.y];
+    const uint32_t* base = (mm.in_mb ? MB : M) + mm.base;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t acc[kMaxMaskWords] = {0, 0, 0, 0};
+    for (int64_t x0 = warp * 32; x0 < n; x0 += nwarps * 32) {
+        const int64_t x = x0 + lane;
+#pragma unroll
+        for (int w = 0; w < kMaxMaskWords; ++w) {
+            if (w >= mm.width) break;
+            const uint32_t val = x < n ? __ldcs(base + x * mm.width + w) : 0u;
+            if (!__any_sync(kFull, val)) continue;
+            for (int bit = 0; bit < 32; ++bit) {
+                const uint32_t c = __popc(__ballot_sync(kFull, (val >> bit) & 1u));
+                if (lane == bit) acc[w] += c;
+            }
+        }
+    }
+#pragma unroll
+    for (int w = 0; w < kMaxMaskWords; ++w) {
+        const int32_t kc = w * 32 + lane;
+        if (w < mm.width && kc < mm.nbits && acc[w]) atomicAdd(sizes + mm.out + (int64_t)kc * mm.stride, acc[w]);
     }
 }
 
@@ -495,6 +813,7 @@ int expand_grid_blocks(int device)
     const size_t smem = sizeof(WarpScratch) * kExpandWarps;
     cudaFuncSetAttribute(k_expand<Pass::Count>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_expand<Pass::Support>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_expand<Pass::Materialize>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_expand<Pass::Support>, kExpandThreads, smem);
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm;
@@ -527,8 +846,83 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     const size_t smem = sizeof(WarpScratch) * kExpandWarps;
     if (pass == Pass::Count)
         k_expand<Pass::Count><<<grid, kExpandThreads, smem, st>>>(a);
-    else
+    else if (pass == Pass::Support)
         k_expand<Pass::Support><<<grid, kExpandThreads, smem, st>>>(a);
+    else
+        k_expand<Pass::Materialize><<<grid, kExpandThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_segmask(DevGraph& g, cudaStream_t st)
+{
+    if (g.n == 0 || g.segw == 0) return cudaSuccess;
+    k_segmask<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.nvl, g.segw, g.offsets, g.adj, g.segmask);
+    return cudaGetLastError();
+}
+
+namespace {
+MaskDev mask_dev(const MaskArgs& x)
+{
+    MaskDev a;
+    a.offsets = x.g->offsets;
+    a.adj = x.g->adj;
+    a.segmask = x.g->segmask;
+    a.n = x.g->n;
+    a.m = x.g->m;
+    a.nvl = x.g->nvl;
+    a.nel = x.g->nel;
+    a.mw = x.g->segw;
+    a.parents = x.parents;
+    a.nparents = x.nparents;
+    a.ntiles = x.ntiles;
+    a.nsweep = x.nsweep;
+    a.in_cols = x.in_col_ptrs;
+    a.counts = x.counts;
+    a.R = x.R;
+    a.H = x.H;
+    a.M = x.M;
+    a.MB = x.MB;
+    a.tile_counter = x.tile_counter;
+    a.scanned = x.scanned;
+    a.status = x.status;
+    return a;
+}
+
+int sm_count()
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+}  // namespace
+
+cudaError_t launch_mask_rows(const MaskArgs& x, cudaStream_t st)
+{
+    if (x.ntiles == 0) return cudaSuccess;
+    const int64_t need = (x.ntiles + kMaskWarps - 1) / kMaskWarps;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    k_mask_rows<<<(int)(need < cap ? need : cap), kMaskWarps * 32, 0, st>>>(mask_dev(x));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mask_sweep(const MaskArgs& x, cudaStream_t st)
+{
+    if (x.nsweep == 0) return cudaSuccess;
+    const int64_t need = (x.nsweep + 7) / 8;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    k_mask_sweep<<<(int)(need < cap ? need : cap), 256, 0, st>>>(mask_dev(x));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mask_sizes(const MaskMatrix* mats, int32_t nmats, const uint32_t* M, const uint32_t* MB,
+                              int32_t n, uint32_t* sizes, cudaStream_t st)
+{
+    const int xblocks = (int)std::min<int64_t>(64, ((int64_t)n + 255) / 256);
+    for (int32_t first = 0; first < nmats; first += 65535) {
+        const int32_t cnt = std::min<int32_t>(65535, nmats - first);
+        k_mask_sizes<<<dim3(xblocks < 1 ? 1 : xblocks, cnt), 256, 0, st>>>(mats + first, M, MB, n, sizes);
+    }
     return cudaGetLastError();
 }
 

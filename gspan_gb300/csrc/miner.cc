@@ -28,7 +28,9 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <functional>
 #include <limits>
+#include <tuple>
 
 namespace gs {
 
@@ -356,14 +358,71 @@ struct Run {
         return GSPAN_OK;
     }
 
+    // Kernel timing (profile mode): event pairs resolved at the next sync.
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_free;
+    std::vector<std::tuple<cudaEvent_t, cudaEvent_t, double*>> ev_pending;
+
+    void tic(cudaEvent_t* a, cudaEvent_t* b)
+    {
+        if (!profile) return;
+        if (ev_free.empty()) {
+            cudaEvent_t x, y;
+            cudaEventCreate(&x);
+            cudaEventCreate(&y);
+            ev_free.emplace_back(x, y);
+        }
+        *a = ev_free.back().first;
+        *b = ev_free.back().second;
+        ev_free.pop_back();
+        cudaEventRecord(*a, s);
+    }
+    void toc(cudaEvent_t a, cudaEvent_t b, double* into)
+    {
+        if (!profile) return;
+        cudaEventRecord(b, s);
+        ev_pending.emplace_back(a, b, into);
+    }
+    void resolve()
+    {
+        for (auto& t : ev_pending) {
+            float ms = 0;
+            cudaEventSynchronize(std::get<1>(t));
+            cudaEventElapsedTime(&ms, std::get<0>(t), std::get<1>(t));
+            *std::get<2>(t) += ms;
+            ev_free.emplace_back(std::get<0>(t), std::get<1>(t));
+        }
+        ev_pending.clear();
+    }
+    void drop_events()
+    {
+        resolve();
+        for (auto& p : ev_free) {
+            cudaEventDestroy(p.first);
+            cudaEventDestroy(p.second);
+        }
+        ev_free.clear();
+    }
+
+    struct Freq {
+        int32_t key;
+        std::vector<CodeEdge> code;
+        uint64_t count;
+        int nvc;
+        int support;
+    };
+
     gspan_status level(int size, std::vector<Parent>& parents, Table& table, std::vector<Parent>& next, Table& out)
     {
-        const int32_t LeLv = g.nel * g.nvl;
-        std::vector<ParentMeta> meta(parents.size());
-        std::vector<int64_t> key_span(parents.size());
-        int64_t nkeys = 0, ntiles = 0;
-        double read_bytes = 0;
-        for (size_t i = 0; i < parents.size(); ++i) {
+        const int32_t K = g.nel * g.nvl;
+        const int np = (int)parents.size();
+        const int mode = ctx->opts.path;
+        const bool mask_possible = g.segw > 0 && mode != 1;
+        const double avg_deg = g.n ? (double)g.m / g.n : 0.0;
+        std::vector<ParentMeta> meta(np);
+        std::vector<int64_t> key_span(np);
+        std::vector<char> use_mask(np, 0);
+        int64_t nkeys = 0;
+        for (int i = 0; i < np; ++i) {
             const std::vector<CodeEdge>& c = parents[i].code;
             ParentMeta& P = meta[i];
             std::memset(&P, 0, sizeof(P));
@@ -399,59 +458,196 @@ struct Run {
             }
             P.row_begin = parents[i].row_begin;
             P.row_end = parents[i].row_end;
-            P.tile_begin = ntiles;
-            ntiles += (P.row_end - P.row_begin + 31) / 32;
             P.key_base = (int32_t)nkeys;
-            key_span[i] = (int64_t)P.nsrc * LeLv + (int64_t)P.nback * g.nel;
+            key_span[i] = (int64_t)P.nsrc * K + (int64_t)P.nback * g.nel;
             nkeys += key_span[i];
             if (nkeys > (int64_t)std::numeric_limits<int32_t>::max())
                 return fail(ctx, GSPAN_ERR_LIMIT, "child key space exceeds 2^31 tuples");
-            read_bytes += (double)(P.row_end - P.row_begin) * (4.0 * nv + 8.0 * P.nsrc);
+            P.bw = (int32_t)(((int64_t)P.nback * g.nel + 31) / 32);
+            if (P.bw < 1) P.bw = 1;
+            // Keys of each source's valid range: to label >= min_label and
+            // (edge label, to label) >= the source's lower bound.
+            for (int s2 = 0; s2 < P.nsrc; ++s2) {
+                const int lo_el = s2 == 0 ? 0 : P.src_el[s2];
+                const int lo_tl = s2 == 0 ? P.min_label : P.src_tl[s2];
+                for (int32_t kc = 0; kc < K && kc < 32 * kMaxMaskWords; ++kc) {
+                    const int el = kc / g.nvl, tl = kc % g.nvl;
+                    if (tl >= P.min_label && (el > lo_el || (el == lo_el && tl >= lo_tl)))
+                        P.range[s2][kc >> 5] |= 1u << (kc & 31);
+                }
+            }
+            if (mask_possible && P.bw <= kMaxMaskWords) {
+                const int64_t rows = P.row_end - P.row_begin;
+                const double dense = (double)P.nsrc * ((double)g.n + g.m) +
+                                     (double)P.nsrc * (nv + 1) * g.n * g.segw + (double)nv * g.n * P.bw;
+                use_mask[i] = mode == 2 || (double)rows * P.nsrc * avg_deg > 2.0 * dense;
+            }
         }
 
-        ParentMeta* d_meta = nullptr;
+        // Groups: mask-path parents, per-candidate parents, and all (materialisation).
+        std::vector<ParentMeta> mg, cg, all = meta;
+        std::vector<int64_t> sz_off(np, -1);
+        int64_t mtiles = 0, ctiles = 0, atiles = 0, nsweep = 0;
+        int64_t r_words = 0, h_words = 0, m_words = 0, b_words = 0, sz_total = 0;
+        std::vector<MaskMatrix> mats;
+        double rows_bytes = 0, cand_read_bytes = 0, all_read_bytes = 0;
+        for (int i = 0; i < np; ++i) {
+            ParentMeta& A = all[i];
+            const int64_t rows = A.row_end - A.row_begin;
+            A.tile_begin = atiles;
+            atiles += (rows + 31) / 32;
+            all_read_bytes += (double)rows * (4.0 * A.nv + 8.0 * A.nsrc);
+            if (use_mask[i]) {
+                ParentMeta P = meta[i];
+                P.tile_begin = mtiles;
+                mtiles += (rows + 31) / 32;
+                P.sweep_begin = nsweep;
+                nsweep += (int64_t)P.nsrc * g.n;
+                P.r_off = r_words;
+                r_words += (int64_t)P.nsrc * g.n;
+                P.h_off = h_words;
+                h_words += (int64_t)P.nsrc * g.m;
+                P.m_off = m_words;
+                m_words += (int64_t)P.nsrc * (P.nv + 1) * g.n * g.segw;
+                P.b_off = b_words;
+                b_words += (int64_t)P.nv * g.n * P.bw;
+                sz_off[i] = sz_total;
+                for (int s2 = 0; s2 < P.nsrc; ++s2)
+                    for (int p = 0; p <= P.nv; ++p)
+                        mats.push_back(MaskMatrix{P.m_off + ((int64_t)s2 * (P.nv + 1) + p) * g.n * g.segw,
+                                                  sz_total + (int64_t)s2 * K * (P.nv + 1) + p, g.segw, K, P.nv + 1, 0});
+                if (P.nback > 0)
+                    for (int p = 0; p < P.nv; ++p)
+                        mats.push_back(MaskMatrix{P.b_off + (int64_t)p * g.n * P.bw,
+                                                  sz_total + (int64_t)P.nsrc * K * (P.nv + 1) + p, P.bw,
+                                                  P.nback * g.nel, P.nv, 1});
+                sz_total += (int64_t)P.nsrc * K * (P.nv + 1) + (int64_t)P.nback * g.nel * P.nv;
+                rows_bytes += (double)rows * (4.0 * P.nv + P.nsrc * (16.0 + 4.0 * g.segw + 4.0 * P.nv * g.segw) +
+                                              8.0 * P.nback);
+                mg.push_back(P);
+            } else {
+                ParentMeta P = meta[i];
+                P.tile_begin = ctiles;
+                ctiles += (rows + 31) / 32;
+                cand_read_bytes += (double)rows * (4.0 * P.nv + 8.0 * P.nsrc);
+                cg.push_back(P);
+            }
+        }
+        st.mask_parents += mg.size();
+        st.candidate_parents += cg.size();
+
         unsigned long long* d_counts = nullptr;
-        GS_CK(dalloc(&d_meta, meta.size(), s), "alloc parents");
-        GS_CK(copy(d_meta, meta.data(), meta.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s),
-              "copy parents");
+        ParentMeta *d_mg = nullptr, *d_cg = nullptr, *d_all = nullptr;
+        uint32_t *d_R = nullptr, *d_H = nullptr, *d_M = nullptr, *d_MB = nullptr, *d_sizes = nullptr;
+        MaskMatrix* d_mats = nullptr;
+        auto release = [&]() {
+            dfree(d_counts, s);
+            dfree(d_mg, s);
+            dfree(d_cg, s);
+            dfree(d_all, s);
+            dfree(d_R, s);
+            dfree(d_H, s);
+            dfree(d_M, s);
+            dfree(d_MB, s);
+            dfree(d_sizes, s);
+            dfree(d_mats, s);
+        };
+        struct Guard {
+            std::function<void()> f;
+            ~Guard() { f(); }
+        } guard{release};
+
         GS_CK(dalloc(&d_counts, (size_t)nkeys, s), "alloc counts");
         GS_CK(cudaMemsetAsync(d_counts, 0, nkeys * 8, s), "clear counts");
-        GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 16, s), "clear counters");
+        GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), s), "clear counters");
 
+        cudaEvent_t e0, e1;
+        if (!mg.empty()) {
+            GS_CK(dalloc(&d_mg, mg.size(), s), "alloc mask parents");
+            GS_CK(copy(d_mg, mg.data(), mg.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
+            GS_CK(dalloc(&d_R, (size_t)r_words, s), "alloc R");
+            GS_CK(dalloc(&d_H, (size_t)h_words, s), "alloc H");
+            GS_CK(dalloc(&d_M, (size_t)std::max<int64_t>(m_words, 1), s), "alloc M");
+            GS_CK(dalloc(&d_MB, (size_t)std::max<int64_t>(b_words, 1), s), "alloc MB");
+            GS_CK(dalloc(&d_sizes, (size_t)std::max<int64_t>(sz_total, 1), s), "alloc sizes");
+            GS_CK(cudaMemsetAsync(d_R, 0, r_words * 4, s), "clear R");
+            GS_CK(cudaMemsetAsync(d_H, 0, h_words * 4, s), "clear H");
+            GS_CK(cudaMemsetAsync(d_M, 0, std::max<int64_t>(m_words, 1) * 4, s), "clear M");
+            GS_CK(cudaMemsetAsync(d_MB, 0, std::max<int64_t>(b_words, 1) * 4, s), "clear MB");
+            GS_CK(cudaMemsetAsync(d_sizes, 0, std::max<int64_t>(sz_total, 1) * 4, s), "clear sizes");
+            GS_CK(dalloc(&d_mats, mats.size(), s), "alloc matrices");
+            GS_CK(copy(d_mats, mats.data(), mats.size() * sizeof(MaskMatrix), cudaMemcpyHostToDevice, s),
+                  "copy matrices");
+            MaskArgs ma{};
+            ma.g = &g;
+            ma.parents = d_mg;
+            ma.nparents = (int32_t)mg.size();
+            ma.ntiles = mtiles;
+            ma.nsweep = nsweep;
+            ma.in_col_ptrs = table.d_cols;
+            ma.counts = d_counts;
+            ma.R = d_R;
+            ma.H = d_H;
+            ma.M = d_M;
+            ma.MB = d_MB;
+            ma.tile_counter = ctx->d_counters + 2;
+            ma.scanned = ctx->d_counters + 3;
+            ma.status = ctx->d_status;
+            tic(&e0, &e1);
+            GS_CK(launch_mask_rows(ma, s), "mask row pass launch");
+            toc(e0, e1, &st.rows_ms);
+            tic(&e0, &e1);
+            GS_CK(launch_mask_sweep(ma, s), "mask sweep launch");
+            toc(e0, e1, &st.sweep_ms);
+            tic(&e0, &e1);
+            GS_CK(launch_mask_sizes(d_mats, (int32_t)mats.size(), d_M, d_MB, g.n, d_sizes, s), "mask sizes launch");
+            toc(e0, e1, &st.domain_ms);
+            st.kernel_launches += 3;
+            st.rows_launches += 1;
+            st.rows_bytes += rows_bytes;
+        }
         ExpandArgs x{};
         x.g = &g;
-        x.parents = d_meta;
-        x.nparents = (int32_t)meta.size();
-        x.ntiles = ntiles;
         x.in_cols = table.ncols;
         x.in_col_ptrs = table.d_cols;
-        x.out_col_ptrs = nullptr;
         x.keys.counts = d_counts;
         x.tile_counter = ctx->d_counters;
         x.scanned = ctx->d_counters + 1;
         x.status = ctx->d_status;
-
-        if (profile) cudaEventRecord(ctx->ev_a, s);
-        GS_CK(launch_expand(x, Pass::Count, s), "count pass launch");
-        if (profile) cudaEventRecord(ctx->ev_b, s);
-        ++st.kernel_launches;
-        std::vector<unsigned long long> counts((size_t)nkeys);
-        unsigned long long ctr[2] = {0, 0};
-        GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read counts");
-        GS_CK(copy(ctr, ctx->d_counters, 16, cudaMemcpyDeviceToHost, s), "read counters");
-        GS_CK(cudaStreamSynchronize(s), "count pass");
-        if (profile) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, ctx->ev_a, ctx->ev_b);
-            st.expand_ms += ms;
-            st.expand_launches += 1;
-            st.expand_bytes += read_bytes + 8.0 * (double)ctr[1];
+        if (!cg.empty()) {
+            GS_CK(dalloc(&d_cg, cg.size(), s), "alloc parents");
+            GS_CK(copy(d_cg, cg.data(), cg.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
+            x.parents = d_cg;
+            x.nparents = (int32_t)cg.size();
+            x.ntiles = ctiles;
+            tic(&e0, &e1);
+            GS_CK(launch_expand(x, Pass::Count, s), "count pass launch");
+            toc(e0, e1, &st.expand_ms);
+            ++st.kernel_launches;
+            ++st.expand_launches;
         }
-        st.scanned_entries += ctr[1];
+        std::vector<unsigned long long> counts((size_t)nkeys);
+        std::vector<uint32_t> sizes((size_t)sz_total);
+        unsigned long long ctr[4] = {0, 0, 0, 0};
+        GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read counts");
+        if (sz_total) GS_CK(copy(sizes.data(), d_sizes, sz_total * 4, cudaMemcpyDeviceToHost, s), "read sizes");
+        GS_CK(copy(ctr, ctx->d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s), "read counters");
+        GS_CK(cudaStreamSynchronize(s), "extension count");
+        resolve();
+        st.scanned_entries += ctr[1] + ctr[3];
+        if (!cg.empty()) st.expand_bytes += cand_read_bytes + 8.0 * (double)ctr[1];
+        if (!mg.empty()) st.sweep_bytes += 12.0 * (double)ctr[3] + 4.0 * (double)r_words;
+        // The mask kernels are done with R, H and M.
+        dfree(d_R, s);
+        dfree(d_H, s);
+        dfree(d_M, s);
+        dfree(d_MB, s);
 
-        const bool mat = size + 1 < k;
-        std::vector<Active> act;
-        for (size_t i = 0; i < parents.size(); ++i) {
+        // Which children count: enough embeddings, minimum code, and (mask
+        // path) support from the domain sizes.
+        std::vector<Freq> freq;
+        std::vector<Active> cand_act;
+        for (int i = 0; i < np; ++i) {
             const ParentMeta& P = meta[i];
             const std::vector<CodeEdge>& c = parents[i].code;
             for (int64_t lk = 0; lk < key_span[i]; ++lk) {
@@ -462,58 +658,133 @@ struct Run {
                 if (cnt < threshold) continue;
                 std::vector<CodeEdge> child = c;
                 int nvc;
-                if (lk < (int64_t)P.nsrc * LeLv) {
-                    const int s2 = (int)(lk / LeLv);
-                    const int el = (int)((lk / g.nvl) % g.nel);
+                int64_t size_at;
+                int stride;
+                if (lk < (int64_t)P.nsrc * K) {
+                    const int s2 = (int)(lk / K);
+                    const int el = (int)((lk % K) / g.nvl);
                     const int tl = (int)(lk % g.nvl);
                     child.push_back(CodeEdge{P.src_v[s2], P.nv, -1, el, tl});
                     nvc = P.nv + 1;
+                    size_at = sz_off[i] + lk * (P.nv + 1);
+                    stride = 1;
                 } else {
-                    const int64_t r = lk - (int64_t)P.nsrc * LeLv;
+                    const int64_t r = lk - (int64_t)P.nsrc * K;
                     const int t = (int)(r / g.nel);
                     const int el = (int)(r % g.nel);
                     child.push_back(CodeEdge{P.vn, P.back_v[t], -1, el, -1});
                     nvc = P.nv;
+                    size_at = sz_off[i] + (int64_t)P.nsrc * K * (P.nv + 1) + r * P.nv;
+                    stride = 1;
                 }
                 if (!is_min_code(child.data(), (int)child.size())) continue;
-                act.push_back(Active{key, std::move(child), cnt, nvc});
+                if (use_mask[i]) {
+                    uint32_t best = std::numeric_limits<uint32_t>::max();
+                    for (int p = 0; p < nvc; ++p) {
+                        const uint32_t v = sizes[(size_t)(size_at + (int64_t)p * stride)];
+                        if (v > 0 && v < best) best = v;
+                    }
+                    const int sup = (int)std::min<uint32_t>(best, 0x7fffffffu);
+                    ++st.support_keys;
+                    if (sup >= min_support) freq.push_back(Freq{key, std::move(child), cnt, nvc, sup});
+                } else {
+                    cand_act.push_back(Active{key, std::move(child), cnt, nvc});
+                }
             }
         }
 
-        ActiveSet as;
-        gspan_status rc = setup_active(act, nkeys, mat, as, out);
-        if (rc != GSPAN_OK) return rc;
-        if (as.nact > 0) {
+        if (!cand_act.empty()) {
+            ActiveSet as;
+            Table none;
+            gspan_status rc = setup_active(cand_act, nkeys, false, as, none);
+            if (rc != GSPAN_OK) {
+                as.release(s);
+                return rc;
+            }
             GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 8, s), "clear tile counter");
+            x.parents = d_cg;
+            x.nparents = (int32_t)cg.size();
+            x.ntiles = ctiles;
             x.keys = LevelKeys{d_counts, as.d_act, as.d_dom, as.d_mat, as.d_cursor};
             x.dom_pool = as.pool;
-            x.out_col_ptrs = mat ? out.d_cols : nullptr;
-            if (profile) cudaEventRecord(ctx->ev_a, s);
+            tic(&e0, &e1);
             GS_CK(launch_expand(x, Pass::Support, s), "support pass launch");
-            if (profile) cudaEventRecord(ctx->ev_b, s);
+            toc(e0, e1, &st.expand_ms);
             ++st.kernel_launches;
+            ++st.expand_launches;
+            st.expand_bytes += cand_read_bytes + 8.0 * (double)ctr[1];
+            std::vector<int> sup;
+            rc = supports(as, sup);
+            resolve();
+            as.release(s);
+            if (rc != GSPAN_OK) return rc;
+            for (size_t a2 = 0; a2 < cand_act.size(); ++a2)
+                if (sup[a2] >= min_support)
+                    freq.push_back(Freq{cand_act[a2].key, std::move(cand_act[a2].code), cand_act[a2].count,
+                                        cand_act[a2].nvc, sup[a2]});
         }
-        std::vector<int> sup;
-        rc = supports(as, sup);
-        if (rc != GSPAN_OK) return rc;
-        if (profile && as.nact > 0) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, ctx->ev_a, ctx->ev_b);
-            st.expand_ms += ms;
-            st.expand_launches += 1;
-            double wbytes = 0;
-            if (mat)
-                for (const Active& a2 : act) wbytes += 4.0 * a2.nvc * (double)a2.count;
-            st.expand_bytes += read_bytes + 8.0 * (double)ctr[1] + wbytes;
+
+        for (const Freq& f : freq) found.push_back(Found{f.code, f.support});
+        if (size + 1 >= k || freq.empty()) return GSPAN_OK;
+
+        // Materialise the frequent children, grouped by tuple (offsets from the
+        // counts: a one-digit counting sort of the candidates by DFS tuple).
+        std::vector<int32_t> act_h((size_t)nkeys, -1);
+        std::vector<long long> mat_h(freq.size());
+        int64_t rows = 0;
+        int ncols = 0;
+        for (size_t a2 = 0; a2 < freq.size(); ++a2) {
+            act_h[freq[a2].key] = (int32_t)a2;
+            mat_h[a2] = rows;
+            rows += (int64_t)freq[a2].count;
+            ncols = std::max(ncols, freq[a2].nvc);
         }
-        for (int32_t a = 0; a < as.nact; ++a) {
-            if (sup[a] < min_support) continue;
-            found.push_back(Found{act[a].code, sup[a]});
-            if (mat) next.push_back(Parent{act[a].code, as.mat[a], as.mat[a] + (int64_t)act[a].count});
-        }
-        as.release(s);
-        dfree(d_counts, s);
-        dfree(d_meta, s);
+        int32_t* d_act = nullptr;
+        long long* d_mat = nullptr;
+        unsigned long long* d_cur = nullptr;
+        GS_CK(dalloc(&d_act, (size_t)nkeys, s), "alloc act");
+        GS_CK(copy(d_act, act_h.data(), act_h.size() * 4, cudaMemcpyHostToDevice, s), "copy act");
+        GS_CK(dalloc(&d_mat, freq.size(), s), "alloc mat");
+        GS_CK(copy(d_mat, mat_h.data(), mat_h.size() * sizeof(long long), cudaMemcpyHostToDevice, s), "copy mat");
+        GS_CK(dalloc(&d_cur, freq.size(), s), "alloc cursor");
+        GS_CK(cudaMemsetAsync(d_cur, 0, freq.size() * 8, s), "clear cursor");
+        out.ncols = ncols;
+        out.rows = rows;
+        out.cols.assign(ncols, nullptr);
+        for (int c2 = 0; c2 < ncols; ++c2) GS_CK(dalloc(&out.cols[c2], (size_t)rows, s), "alloc level table");
+        GS_CK(dalloc(&out.d_cols, (size_t)ncols, s), "alloc column table");
+        GS_CK(copy(out.d_cols, out.cols.data(), ncols * sizeof(int32_t*), cudaMemcpyHostToDevice, s),
+              "copy column table");
+        GS_CK(dalloc(&d_all, all.size(), s), "alloc parents");
+        GS_CK(copy(d_all, all.data(), all.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
+        GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 16, s), "clear counters");
+        x.parents = d_all;
+        x.nparents = (int32_t)all.size();
+        x.ntiles = atiles;
+        x.keys = LevelKeys{d_counts, d_act, nullptr, d_mat, d_cur};
+        x.out_col_ptrs = out.d_cols;
+        tic(&e0, &e1);
+        GS_CK(launch_expand(x, Pass::Materialize, s), "materialise launch");
+        toc(e0, e1, &st.materialize_ms);
+        ++st.kernel_launches;
+        ++st.materialize_launches;
+        unsigned long long scanned = 0;
+        GS_CK(copy(&scanned, ctx->d_counters + 1, 8, cudaMemcpyDeviceToHost, s), "read counters");
+        uint32_t mstatus = 0;
+        GS_CK(copy(&mstatus, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
+        GS_CK(cudaStreamSynchronize(s), "materialise");
+        resolve();
+        if (mstatus) return fail(ctx, GSPAN_ERR_DEVICE, "kernel status word " + std::to_string(mstatus));
+        st.scanned_entries += scanned;
+        st.materialized_rows += (uint64_t)rows;
+        double wbytes = 0;
+        for (const Freq& f : freq) wbytes += 4.0 * f.nvc * (double)f.count;
+        st.materialize_bytes += all_read_bytes + 8.0 * (double)scanned + wbytes;
+        for (size_t a2 = 0; a2 < freq.size(); ++a2)
+            next.push_back(Parent{freq[a2].code, mat_h[a2], mat_h[a2] + (int64_t)freq[a2].count});
+        dfree(d_act, s);
+        dfree(d_mat, s);
+        dfree(d_cur, s);
         return GSPAN_OK;
     }
 };
@@ -551,6 +822,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, int min_support, gsp
         ++size;
     }
     table.release(run.s);
+    run.drop_events();
     run.st.levels = run.found.empty() ? 0 : size;
     if (rc != GSPAN_OK) {
         cudaStreamSynchronize(run.s);

@@ -36,7 +36,7 @@ struct gspan_ctx {
     int expand_blocks = 0;
     // Small device words reused by every pass.
     uint32_t* d_status = nullptr;
-    unsigned long long* d_counters = nullptr;   // [0] tile counter, [1] scanned entries
+    unsigned long long* d_counters = nullptr;   // [0],[2] tile counters, [1],[3] scanned entries
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_c = nullptr, ev_d = nullptr;
     int live_graphs = 0;
 };

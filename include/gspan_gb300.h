@@ -57,6 +57,8 @@ typedef struct gspan_opts {
                                     0 selects the default (1.0) */
     double mem_fraction;         /* share of free device memory the miner may hold (0 = 0.85) */
     int32_t profile;             /* 1: time every kernel launch with CUDA events into gspan_stats */
+    int32_t path;                /* extension kernels: 0 auto, 1 per-candidate only, 2 mask path wherever the
+                                    label space allows (both give identical results) */
 } gspan_opts;
 
 /* Run statistics.  Counts are exact and identical to those of the reference's
@@ -72,14 +74,25 @@ typedef struct gspan_stats {
     uint64_t kernel_launches;    /* kernels of this library launched during gspan_mine */
     int32_t levels;              /* deepest pattern size reached */
     double mine_ms;              /* host wall time of gspan_mine */
-    /* profile == 1 only: per kernel family, CUDA-event time summed over launches */
-    double expand_ms;            /* extension kernels (count + support/materialise passes) */
-    uint64_t expand_launches;
-    double expand_bytes;         /* algorithmic bytes moved by those launches */
-    double seed_ms;
-    double domain_ms;            /* domain-size reductions */
     uint64_t h2d_bytes;          /* host->device bytes copied by gspan_mine */
     uint64_t d2h_bytes;          /* device->host bytes copied by gspan_mine */
+    uint64_t mask_parents;       /* parent patterns extended by the mask kernels */
+    uint64_t candidate_parents;  /* parent patterns extended by the per-candidate kernels */
+    /* Per kernel family: launches, algorithmic bytes, and (profile == 1 only)
+     * CUDA-event time summed over launches. */
+    double expand_ms;            /* per-candidate kernels, Count and Support passes */
+    uint64_t expand_launches;
+    double expand_bytes;
+    double rows_ms;              /* mask path: row pass */
+    uint64_t rows_launches;
+    double rows_bytes;
+    double sweep_ms;             /* mask path: adjacency sweep */
+    double sweep_bytes;
+    double materialize_ms;       /* child-row scatter of frequent children */
+    uint64_t materialize_launches;
+    double materialize_bytes;
+    double seed_ms;
+    double domain_ms;            /* domain-size reductions */
 } gspan_stats;
 
 typedef struct gspan_ctx gspan_ctx;

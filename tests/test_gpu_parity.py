@@ -15,10 +15,12 @@ from helpers import (ROOT, golden_cases, golden_graph, golden_lines, lines_of, r
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def miner():
+@pytest.fixture(scope="module", params=[0, 1, 2], ids=["auto", "per-candidate", "mask"])
+def miner(request):
+    """One context per extension-kernel choice: automatic, per-candidate only,
+    mask path wherever the label space allows.  All must agree bit for bit."""
     from gspan_gb300 import Miner
-    m = Miner()
+    m = Miner(path=request.param)
     yield m
     m.close()
 
