@@ -132,6 +132,22 @@ class ClockSampler:
                 if any(r[3].replace('.', '').isdigit() for r in rows) else None}
 
 
+def max_over_ranks(values, device=None):
+    """Element-wise MAX over all ranks (the values unchanged without a process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_value(world: int, units_per_rank: float, slowest_ms: float) -> float:
+    """Whole-job throughput of `world` replicas: every rank's units over the slowest time."""
+    return world * units_per_rank / (slowest_ms / 1e3)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -245,16 +261,13 @@ def gpu_arm(args, wl) -> None:
     total_ms = sum(step_ms)
     e2e_total = sum(e2e_ms)
     ext = sum(s["extended"] for s in stats)
-    if world > 1:
-        t = torch.tensor([total_ms, e2e_total], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms, e2e_total = float(t[0]), float(t[1])
+    total_ms, e2e_total = max_over_ranks([total_ms, e2e_total], device=dev)
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
-    value = world * ext / (total_ms / 1e3)
-    e2e_value = world * ext / (e2e_total / 1e3)
+    value = replica_value(world, ext, total_ms)
+    e2e_value = replica_value(world, ext, e2e_total)
     # Dominant kernel family by CUDA-event time over the timed steps.
     fams = {"k_mask_rows (mask path row pass)": ("rows_ms", "rows_bytes", "rows_launches"),
             "k_expand Count/Support (per-candidate path)": ("expand_ms", "expand_bytes", "expand_launches"),

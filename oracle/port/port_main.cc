@@ -1,6 +1,8 @@
 // Test infrastructure only: command-line front end of the CPU oracle.
 //
 //   fsm_port <graph.bin> <min_support> <k> [--stats]
+//   fsm_port --canonical      (codes on stdin, one per line: len then 5 ints
+//                              per edge; prints 1 or 0 per line)
 //
 // Prints one line per frequent canonical pattern in the reference's format and
 // order (gspan.cu:67-77), then the reference's timing line (fsm.cu:37-40).
@@ -13,8 +15,21 @@
 #include <cstring>
 #include <omp.h>
 
+static int canonical_mode()
+{
+    int len;
+    while (std::scanf("%d", &len) == 1) {
+        port::Code code(len);
+        for (auto& e : code)
+            if (std::scanf("%d%d%d%d%d", &e.from, &e.to, &e.fl, &e.el, &e.tl) != 5) return 1;
+        std::printf("%d\n", port::is_canonical(code) ? 1 : 0);
+    }
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
+    if (argc == 2 && std::strcmp(argv[1], "--canonical") == 0) return canonical_mode();
     if (argc < 4) {
         std::printf("usage: %s input_graph min_support k [--stats]\n", argv[0]);
         return 2;
