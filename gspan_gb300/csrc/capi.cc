@@ -196,6 +196,15 @@ gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t n, int32_t m, const int3
     std::vector<int32_t> vrank;
     rank_labels(vlabels, (size_t)n, 1, g.vlabel_of_rank, &vrank);
     rank_labels(m > 0 ? &edges[0].label : nullptr, (size_t)m, 3, g.elabel_of_rank, nullptr);
+    {
+        double d1 = 0, d2 = 0;
+        for (int32_t v = 0; v < n; ++v) {
+            const double d = (double)offsets[v + 1] - offsets[v];
+            d1 += d;
+            d2 += d * d;
+        }
+        g.edge_biased_degree = d1 > 0 ? d2 / d1 : 0.0;
+    }
     g.nvl = (int32_t)g.vlabel_of_rank.size();
     g.nel = (int32_t)g.elabel_of_rank.size();
     if (g.nvl > 0xFFFF || g.nel > 0xFFFF) {

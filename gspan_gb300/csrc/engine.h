@@ -50,6 +50,9 @@ struct DevGraph {
     // space nel * nvl fits kMaxMaskWords words, else null (segw = 0).
     uint32_t* segmask = nullptr;
     int32_t segw = 0;
+    // Mean degree of a vertex reached through an edge (sum d^2 / sum d): the
+    // expected adjacency length behind an embedding's vertex.
+    double edge_biased_degree = 0;
     std::vector<int32_t> vlabel_of_rank, elabel_of_rank;
 };
 

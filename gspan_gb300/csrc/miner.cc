@@ -417,7 +417,6 @@ struct Run {
         const int np = (int)parents.size();
         const int mode = ctx->opts.path;
         const bool mask_possible = g.segw > 0 && mode != 1;
-        const double avg_deg = g.n ? (double)g.m / g.n : 0.0;
         std::vector<ParentMeta> meta(np);
         std::vector<int64_t> key_span(np);
         std::vector<char> use_mask(np, 0);
@@ -480,7 +479,7 @@ struct Run {
                 const int64_t rows = P.row_end - P.row_begin;
                 const double dense = (double)P.nsrc * ((double)g.n + g.m) +
                                      (double)P.nsrc * (nv + 1) * g.n * g.segw + (double)nv * g.n * P.bw;
-                use_mask[i] = mode == 2 || (double)rows * P.nsrc * avg_deg > 2.0 * dense;
+                use_mask[i] = mode == 2 || (double)rows * P.nsrc * g.edge_biased_degree > 2.0 * dense;
             }
         }
 
