@@ -99,6 +99,9 @@ _lib.gspan_graph_free.restype = ctypes.c_int
 _lib.gspan_mine.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, EMIT_FN,
                             ctypes.c_void_p, ctypes.POINTER(Stats)]
 _lib.gspan_mine.restype = ctypes.c_int
+_lib.gspan_table_support.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
+                                     ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]
+_lib.gspan_table_support.restype = ctypes.c_int
 _lib.gspan_is_canonical.argtypes = [ctypes.POINTER(PatternEdge), ctypes.c_int32, _i32p]
 _lib.gspan_is_canonical.restype = ctypes.c_int
 _lib.gspan_status_string.argtypes = [ctypes.c_int]
@@ -110,8 +113,8 @@ _lib.gspan_max_pattern_edges.restype = ctypes.c_int32
 
 # Every symbol include/gspan_gb300.h declares (checked by the tests).
 ABI_SYMBOLS = ("gspan_opts_default", "gspan_ctx_create", "gspan_ctx_destroy", "gspan_graph_upload",
-               "gspan_graph_free", "gspan_mine", "gspan_is_canonical", "gspan_status_string",
-               "gspan_last_error", "gspan_max_pattern_edges")
+               "gspan_graph_free", "gspan_mine", "gspan_table_support", "gspan_is_canonical",
+               "gspan_status_string", "gspan_last_error", "gspan_max_pattern_edges")
 
 Code = tuple  # tuple of (from, to, from_label, edge_label, to_label)
 
@@ -210,6 +213,20 @@ class Miner:
         if rc != GSPAN_OK:
             raise self._err(rc, "gspan_mine")
         return out, st.as_dict()
+
+    def table_support(self, cols, nr_nodes: int):
+        """MNI support of an embedding table on the device (the reference's
+        support_gpu for a column table).  ``cols``: CUDA int32 tensors of equal
+        length, one per pattern vertex.  Returns (domain sizes, support)."""
+        import torch
+        nrows = int(cols[0].numel()) if cols else 0
+        ptrs = (ctypes.c_void_p * len(cols))(*[c.data_ptr() for c in cols])
+        out = torch.empty(len(cols) + 1, dtype=torch.int32, device=cols[0].device if cols else "cuda")
+        rc = _lib.gspan_table_support(self._ctx, int(nr_nodes), ptrs, len(cols), nrows, out.data_ptr())
+        if rc != GSPAN_OK:
+            raise self._err(rc, "gspan_table_support")
+        host = out.cpu().tolist()
+        return host[:-1], host[-1]
 
     def fsm(self, g: CSR, k: int, min_support: int):
         """Upload, mine, free: the reference's ``fsm`` as one call."""

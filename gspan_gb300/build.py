@@ -26,7 +26,8 @@ OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libgspan_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels.cu", "miner.cc", "capi.cc", "canonical.cc", "host_graph.cc", "host_fsm.cc"]
+SOURCES = ["kernels.cu", "table_support.cu", "miner.cc", "capi.cc", "canonical.cc", "host_graph.cc",
+           "host_fsm.cc"]
 TOOLS = {"fsm": "tools/fsm_main.cc", "convert": "tools/convert_main.cc"}
 
 

@@ -124,6 +124,17 @@ gspan_status gspan_graph_free(gspan_ctx* ctx, gspan_graph* graph);
 gspan_status gspan_mine(gspan_ctx* ctx, const gspan_graph* graph, int32_t k, int32_t min_support,
                         gspan_emit_fn emit, void* user, gspan_stats* stats);
 
+/* MNI support of an embedding table in device memory (the reference's
+ * support_gpu, gspan.cu:200-289, for a column table): `cols` is a host array
+ * of `ncols` (1..16) device pointers, each to `nrows` int32 vertex ids in
+ * [0, nr_nodes), one column per pattern vertex.  Writes to the device array
+ * `out[ncols + 1]` the distinct-id count of every column and, at out[ncols],
+ * the support: the smallest non-zero count (0x7fffffff when nrows == 0).
+ * Runs on the context's stream and returns when `out` is ready.  An id
+ * outside [0, nr_nodes) returns INVALID. */
+gspan_status gspan_table_support(gspan_ctx* ctx, int32_t nr_nodes, const int32_t* const* cols, int32_t ncols,
+                                 int64_t nrows, uint32_t* out);
+
 /* Host-only: whether `code` is a minimum DFS code by the reference's test
  * (gspan.cu:586-606).  Writes 1 or 0 to *out. */
 gspan_status gspan_is_canonical(const gspan_pattern_edge* code, int32_t len, int32_t* out);
