@@ -102,6 +102,9 @@ _lib.gspan_mine.restype = ctypes.c_int
 _lib.gspan_table_support.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]
 _lib.gspan_table_support.restype = ctypes.c_int
+_lib.gspan_table_support_noalloc.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                                             ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+_lib.gspan_table_support_noalloc.restype = ctypes.c_int
 _lib.gspan_is_canonical.argtypes = [ctypes.POINTER(PatternEdge), ctypes.c_int32, _i32p]
 _lib.gspan_is_canonical.restype = ctypes.c_int
 _lib.gspan_status_string.argtypes = [ctypes.c_int]
@@ -113,7 +116,8 @@ _lib.gspan_max_pattern_edges.restype = ctypes.c_int32
 
 # Every symbol include/gspan_gb300.h declares (checked by the tests).
 ABI_SYMBOLS = ("gspan_opts_default", "gspan_ctx_create", "gspan_ctx_destroy", "gspan_graph_upload",
-               "gspan_graph_free", "gspan_mine", "gspan_table_support", "gspan_is_canonical",
+               "gspan_graph_free", "gspan_mine", "gspan_table_support", "gspan_table_support_noalloc",
+               "gspan_is_canonical",
                "gspan_status_string", "gspan_last_error", "gspan_max_pattern_edges")
 
 Code = tuple  # tuple of (from, to, from_label, edge_label, to_label)

@@ -6,6 +6,7 @@
 #include "miner.h"
 
 #include <algorithm>
+#include <mutex>
 
 namespace gs {
 namespace {
@@ -118,4 +119,101 @@ extern "C" gspan_status gspan_table_support(gspan_ctx* ctx, int32_t nr_nodes, co
     if (e2 != cudaSuccess) return gs::cuda_fail(ctx, e2, "table support");
     if (status) return gs::fail(ctx, GSPAN_ERR_INVALID, "table support: a vertex id is outside [0, nr_nodes)");
     return GSPAN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of gspan_table_support.
+//
+// Some callers cannot let this library allocate device memory: a serving
+// process that reserved its whole device-memory budget at start-up and must
+// not grow or fragment it later, a latency-critical loop that cannot afford
+// the device-wide synchronisation cudaMalloc/cudaFree may cause, or a host
+// application whose own allocator owns every byte of device memory.  For
+// them the domain bitmaps live in a fixed array that is part of this
+// library's device image, so the call itself allocates nothing.
+//
+// The array is 8 MiB on every GPU that loads the library, held until the
+// process exits.  Its first 64 words are a header (word 0: bad-id flag); the
+// bitmaps follow, so ncols * ceil(nr_nodes / 32) may be at most
+// kNoAllocBitmapWords (2,097,088 words: e.g. 16 columns of 4.19M vertices).
+// Every call uses the same array and leaves its bitmaps behind; each call
+// clears the part it uses before filling it.  Calls whose work overlaps on
+// the GPU (another stream, another host thread) race on the array.
+
+namespace gs {
+namespace {
+
+constexpr size_t kNoAllocScratchWords = (size_t)2 << 20;   // 8 MiB
+constexpr size_t kNoAllocHeaderWords = 64;                 // 256 bytes
+constexpr size_t kNoAllocBitmapWords = kNoAllocScratchWords - kNoAllocHeaderWords;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) uint32_t g_table_scratch[kNoAllocScratchWords];
+
+std::mutex g_scratch_mu;
+uint32_t* g_scratch_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_table_scratch on device `dev` (which must be current).
+// In host code the symbol is only a host-side stand-in, so the address is
+// fetched once per device with cudaGetSymbolAddress and cached.
+gspan_status scratch_for(int dev, uint32_t** out)
+{
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return GSPAN_ERR_LIMIT;
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_table_scratch);
+        if (e != cudaSuccess || !p) return GSPAN_ERR_CUDA;
+        g_scratch_addr[dev] = static_cast<uint32_t*>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return GSPAN_OK;
+}
+
+__global__ void k_scratch_clear(uint32_t* __restrict__ words, int64_t count)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        words[i] = 0u;
+}
+
+// Like k_table_min, but out[ncols] = 0xFFFFFFFF when the fill saw an id
+// outside [0, nr_nodes) (the call is asynchronous and cannot return it).
+__global__ void k_table_min_flagged(int32_t ncols, const uint32_t* __restrict__ flag, uint32_t* out)
+{
+    uint32_t best = 0x7fffffffu;
+    for (int c = 0; c < ncols; ++c)
+        if (out[c] > 0 && out[c] < best) best = out[c];
+    out[ncols] = *flag ? 0xFFFFFFFFu : best;
+}
+
+}  // namespace
+}  // namespace gs
+
+extern "C" gspan_status gspan_table_support_noalloc(int32_t nr_nodes, const int32_t* const* cols, int32_t ncols,
+                                                    int64_t nrows, uint32_t* out, void* stream)
+{
+    gs::TableCols t{};
+    if (gs::check_table_args(nr_nodes, cols, ncols, nrows, out, &t) != GSPAN_OK) return GSPAN_ERR_INVALID;
+    const size_t words = ((size_t)nr_nodes + 31) / 32;
+    if ((size_t)ncols * words > gs::kNoAllocBitmapWords) return GSPAN_ERR_LIMIT;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GSPAN_ERR_NO_DEVICE;
+    uint32_t* scratch = nullptr;
+    const gspan_status rc = gs::scratch_for(dev, &scratch);
+    if (rc != GSPAN_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t* flag = scratch;
+    uint32_t* bits = scratch + gs::kNoAllocHeaderWords;
+    const int64_t used = (int64_t)gs::kNoAllocHeaderWords + (int64_t)ncols * (int64_t)words;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = (int)std::min<int64_t>((used + 255) / 256, (int64_t)(sms > 0 ? sms : 1) * 8);
+    gs::k_scratch_clear<<<grid, 256, 0, s>>>(scratch, used);
+    if (nrows > 0) {
+        const int fgrid = (int)std::min<int64_t>((nrows + 255) / 256, (int64_t)(sms > 0 ? sms : 1) * 8);
+        gs::k_table_fill<<<fgrid, 256, 0, s>>>(t, ncols, nrows, nr_nodes, (uint32_t)words, bits, flag);
+    }
+    gs::k_table_sizes<<<ncols, 256, 0, s>>>((uint32_t)words, bits, out);
+    gs::k_table_min_flagged<<<1, 1, 0, s>>>(ncols, flag, out);
+    return cudaGetLastError() == cudaSuccess ? GSPAN_OK : GSPAN_ERR_CUDA;
 }

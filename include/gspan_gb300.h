@@ -135,6 +135,26 @@ gspan_status gspan_mine(gspan_ctx* ctx, const gspan_graph* graph, int32_t k, int
 gspan_status gspan_table_support(gspan_ctx* ctx, int32_t nr_nodes, const int32_t* const* cols, int32_t ncols,
                                  int64_t nrows, uint32_t* out);
 
+/* Allocation-free gspan_table_support.  No counterpart in the reference: it is
+ * for callers that cannot let a library allocate device memory - a process
+ * that fixed its device-memory budget at start-up, a latency-critical loop
+ * that cannot take the synchronisation cudaMalloc/cudaFree may cause, or an
+ * application whose own allocator owns all device memory.  It needs no
+ * context and allocates nothing: the domain bitmaps live in an 8 MiB array
+ * compiled into the library, which every GPU that loads the library holds
+ * until the process exits.
+ *   - Same inputs and outputs as gspan_table_support, on the current device,
+ *     enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream)
+ *     and asynchronous: `out` is ready when the stream reaches this work.
+ *   - ncols * ceil(nr_nodes / 32) must be at most 2,097,088 (LIMIT otherwise).
+ *   - An id outside [0, nr_nodes) cannot be returned as an error by an
+ *     asynchronous call; out[ncols] is then 0xFFFFFFFF.
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture on that device.
+ *   - All calls share the array: calls whose GPU work overlaps race. */
+gspan_status gspan_table_support_noalloc(int32_t nr_nodes, const int32_t* const* cols, int32_t ncols,
+                                         int64_t nrows, uint32_t* out, void* stream);
+
 /* Host-only: whether `code` is a minimum DFS code by the reference's test
  * (gspan.cu:586-606).  Writes 1 or 0 to *out. */
 gspan_status gspan_is_canonical(const gspan_pattern_edge* code, int32_t len, int32_t* out);
