@@ -71,7 +71,9 @@ void free_graph(gspan_graph* gr, cudaStream_t st)
     if (g.src) cudaFreeAsync(g.src, st);
     if (g.vrank) cudaFreeAsync(g.vrank, st);
     if (g.segmask) cudaFreeAsync(g.segmask, st);
+    if (g.selfloop) cudaFreeAsync(g.selfloop, st);
     g.segmask = nullptr;
+    g.selfloop = nullptr;
     g.offsets = nullptr;
     g.adj = nullptr;
     g.src = nullptr;
@@ -274,6 +276,24 @@ gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t n, int32_t m, const int3
         delete gr;
         return fail(ctx, GSPAN_ERR_INVALID, "malformed graph: offsets not monotone, an entry's `from` differs from "
                                             "its vertex, or a `to` is out of range");
+    }
+    // Self-loop bits and the symmetry check, on the validated adjacency.
+    {
+        const size_t words = ((size_t)n + 31) / 32 + 1;
+        cudaError_t e2;
+        uint32_t flags = 0;
+        if ((e2 = cudaMallocAsync(&g.selfloop, words * 4, s)) != cudaSuccess ||
+            (e2 = cudaMemsetAsync(g.selfloop, 0, words * 4, s)) != cudaSuccess ||
+            (e2 = cudaMemsetAsync(ctx->d_status, 0, 4, s)) != cudaSuccess ||
+            (e2 = gs::launch_graph_flags(g, ctx->d_status, s)) != cudaSuccess ||
+            (e2 = cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+            (e2 = cudaStreamSynchronize(s)) != cudaSuccess) {
+            free_graph(gr, s);
+            cudaStreamSynchronize(s);
+            delete gr;
+            return cuda_fail(ctx, e2, "graph flags");
+        }
+        g.symmetric = !(flags & gs::kErrAsymmetric);
     }
     ++ctx->live_graphs;
     *out = gr;

@@ -33,6 +33,7 @@ enum : uint32_t {
     kErrHashFull = 1u << 0,     // a hashset probe ran through its whole table
     kErrBadGraph = 1u << 1,     // upload validation: offsets or entries inconsistent
     kErrCursor = 1u << 2,       // a materialisation cursor ran past its reserved rows
+    kErrAsymmetric = 1u << 3,   // upload: an entry without its reverse entry (not an error)
 };
 
 // The graph in HBM.  Labels are replaced by their rank among the distinct
@@ -50,6 +51,11 @@ struct DevGraph {
     // space nel * nvl fits kMaxMaskWords words, else null (segw = 0).
     uint32_t* segmask = nullptr;
     int32_t segw = 0;
+    // Bit v set when vertex v has an entry to itself.
+    uint32_t* selfloop = nullptr;
+    // Every entry u->x with edge label l has a reverse entry x->u with label l
+    // (checked at upload; true for every graph built by the text loader).
+    bool symmetric = false;
     // Mean degree of a vertex reached through an edge (sum d^2 / sum d): the
     // expected adjacency length behind an embedding's vertex.
     double edge_biased_degree = 0;
@@ -100,25 +106,24 @@ struct ParentMeta {
     int8_t e_from[kMaxE];       // parent code edges, for the has_edge test
     int8_t e_to[kMaxE];
     int16_t e_el[kMaxE];
-    // Mask path (see k_mask_rows): offsets of this parent's dense arrays.
+    uint16_t src_adj[kMaxV];    // per source: pattern vertices joined to it by a code edge
+    // Materialisation: the frequent forward tuples as (source, el * nvl + tl),
+    // scanned segment by segment; nmseg = -1 scans every source's full range.
+    int16_t nmseg;
+    int16_t mseg_s[kMaxV];
+    uint32_t mseg_kc[kMaxV];
+    // Mask path (see k_mask_rows): offsets of this parent's arrays in the
+    // buffers of its parent group.
     int32_t bw;                 // words per backward-key mask
-    int64_t sweep_begin;        // first (source, vertex) task of this parent in the sweep
+    int32_t ps_begin;           // first (parent, source) slot of this parent in the group
+    int32_t t_cap;              // touched-list capacity per source: min(rows, n)
+    int64_t t_off;              // touched lists: nsrc x t_cap vertices
     int64_t r_off;              // R: nsrc x n row counters
     int64_t h_off;              // H: nsrc x m entry counters
     int64_t m_off;              // M: nsrc x (nv+1) x n x segw words
     int64_t b_off;              // MB: nv x n x bw words
+    int64_t sz_off;             // domain sizes: nsrc*K*(nv+1) forward, then nback*nel*nv backward
     uint32_t range[kMaxV][kMaxMaskWords];   // per source: keys inside its valid range
-};
-
-// One key-mask matrix whose column popcounts are domain sizes: `n` vertices x
-// `width` words at `base`; column kc adds to sizes[out + kc * stride].
-struct MaskMatrix {
-    int64_t base;
-    int64_t out;
-    int32_t width;
-    int32_t nbits;
-    int32_t stride;
-    int32_t in_mb;               // 1: offset into MB (backward keys), 0: into M
 };
 
 // Per-level key space arrays on the device.
@@ -164,24 +169,31 @@ int expand_grid_blocks(int device);
 // Mask path.
 struct MaskArgs {
     const DevGraph* g;
-    const ParentMeta* parents;   // device, mask-path parents only
+    const ParentMeta* parents;   // device, one group of mask-path parents
     int32_t nparents;
     int64_t ntiles;
-    int64_t nsweep;              // total (parent, source, vertex) sweep tasks
     int32_t* const* in_col_ptrs;
     unsigned long long* counts;  // level key space
-    uint32_t* R;
-    uint32_t* H;
-    uint32_t* M;
-    uint32_t* MB;
+    uint32_t* sizes;             // domain sizes, indexed from ParentMeta::sz_off
+    uint32_t* R;                 // zero on entry; the sweep leaves it zero
+    uint32_t* H;                 // zero on entry; the sweep leaves it zero
+    uint32_t* M;                 // zero on entry
+    uint32_t* MB;                // zero on entry
+    int32_t* touched;
+    uint32_t* tcount;            // [nps], zero on entry
+    const int32_t* ps_parent;    // [nps] parent index of each (parent, source) slot
+    int32_t nps;
+    unsigned long long* tprefix; // [nps + 1] scratch
     unsigned long long* tile_counter;
-    unsigned long long* scanned;  // adjacency entries read by the sweep
+    unsigned long long* scanned; // adjacency entries read by the sweep
     uint32_t* status;
 };
 cudaError_t launch_segmask(DevGraph& g, cudaStream_t st);
+// Self-loop bitmap (zeroed by the caller) and the symmetry check: sets
+// kErrAsymmetric in *status when some entry has no reverse entry.
+cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st);
 cudaError_t launch_mask_rows(const MaskArgs& a, cudaStream_t st);
+// Prefix of the touched lists, then the sweep (two launches).
 cudaError_t launch_mask_sweep(const MaskArgs& a, cudaStream_t st);
-cudaError_t launch_mask_sizes(const MaskMatrix* mats, int32_t nmats, const uint32_t* M, const uint32_t* MB,
-                              int32_t n, uint32_t* sizes, cudaStream_t st);
 
 }  // namespace gs

@@ -276,19 +276,31 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
 
         for (int p = 0; p < nv; ++p) W.img[lane][p] = live ? __ldcs(a.in_cols[p] + row) : -1;
 
+        // Ranges to scan per row: one per source (the source's valid suffix),
+        // or, when materialising with few frequent tuples, one per frequent
+        // tuple segment (slot q covers source mseg_s[q], tuple mseg_kc[q]).
+        const bool segs = kPass == Pass::Materialize && P.nmseg >= 0;
+        const int nslot = segs ? P.nmseg : nsrc;
         int32_t work = 0;
-        for (int s = 0; s < nsrc; ++s) {
+        for (int q = 0; q < nslot; ++q) {
             int32_t st = 0, c = 0;
             if (live) {
-                const int32_t u = W.img[lane][P.src_v[s]];
+                const int sq = segs ? P.mseg_s[q] : q;
+                const int32_t u = W.img[lane][P.src_v[sq]];
                 const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
-                const uint64_t lo_key = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
-                                               : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
-                st = lower_bound_entry(a.adj, b, e, lo_key);
-                c = e - st;
+                if (segs) {
+                    const uint32_t el = P.mseg_kc[q] / (uint32_t)a.nvl, tl = P.mseg_kc[q] % (uint32_t)a.nvl;
+                    st = lower_bound_entry(a.adj, b, e, pack_entry(el, tl, 0));
+                    c = lower_bound_entry(a.adj, st, e, pack_entry(el, tl + 1, 0)) - st;
+                } else {
+                    const uint64_t lo_key = sq == 0 ? pack_entry(0, (uint32_t)min_label, 0)
+                                                    : pack_entry((uint32_t)P.src_el[sq], (uint32_t)P.src_tl[sq], 0);
+                    st = lower_bound_entry(a.adj, b, e, lo_key);
+                    c = e - st;
+                }
             }
-            W.start[lane][s] = st;
-            W.cnt[lane][s] = c;
+            W.start[lane][q] = st;
+            W.cnt[lane][q] = c;
             work += c;
         }
         int32_t incl = work;
@@ -389,7 +401,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                 bool fresh = tl >= min_label;
                 for (int p = 0; p < nv; ++p) fresh &= W.img[owner][p] != (int32_t)to;
                 ok = fresh;
-                key = key_base + s * LeLv + (int32_t)entry_el(e) * a.nvl + tl;
+                key = key_base + (segs ? P.mseg_s[s] : s) * LeLv + (int32_t)entry_el(e) * a.nvl + tl;
             }
             const unsigned mask = __ballot_sync(kFull, ok);
             if (kPass == Pass::Count) {
@@ -449,8 +461,12 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
 // R[u] - H[e], and the new vertex's domain is {to(e) : R[u] > H[e]}.  An old
 // vertex p's domain for (s, c) is {img_r(p) : row r has an entry of
 // seg(u_r, c) outside its images}; the row pass ORs the set of such c (a
-// bitmask over the tuple space) into M[p][img_r(p)], so a domain size is the
-// popcount of one bit column of M.  All of it is exact.
+// bitmask over the tuple space) into M[p][img_r(p)].  Domain sizes are counted
+// as bits first appear in M, so no pass over M is needed.  All of it is exact.
+//
+// The row pass lists every vertex whose R goes 0 -> 1 (`touched`), so the
+// sweep visits only those vertices; it also resets the R and H entries it
+// reads, leaving both arrays zero for the next group of parents.
 
 constexpr int kMaskWarps = 8;
 
@@ -458,25 +474,50 @@ struct MaskDev {
     const int32_t* offsets;
     const uint64_t* adj;
     const uint32_t* segmask;
+    const uint32_t* selfloop;
+    bool symmetric;
     int32_t n, m, nvl, nel, mw;
     const ParentMeta* parents;
     int32_t nparents;
     int64_t ntiles;
-    int64_t nsweep;
     int32_t* const* in_cols;
     unsigned long long* counts;
+    uint32_t* sizes;
     uint32_t* R;
     uint32_t* H;
     uint32_t* M;
     uint32_t* MB;
+    int32_t* touched;
+    uint32_t* tcount;
+    const int32_t* ps_parent;
+    int32_t nps;
+    unsigned long long* tprefix;
     unsigned long long* tile_counter;
     unsigned long long* scanned;
     uint32_t* status;
 };
 
-__device__ __forceinline__ void or_words(uint32_t* p, uint32_t bits)
+// OR `bits` into *p and return the bits that were not set before (a word
+// already holding all of them costs one L2 read and no atomic).
+__device__ __forceinline__ uint32_t or_fresh(uint32_t* p, uint32_t bits)
 {
-    if (bits && (__ldcg(p) & bits) != bits) atomicOr(p, bits);
+    if (!bits || (__ldcg(p) & bits) == bits) return 0u;
+    return bits & ~atomicOr(p, bits);
+}
+
+// Warp-wide: every bit b newly set by any lane in `word` adds the number of
+// such lanes to its tuple's domain size sizes[out + (word * 32 + b) * stride].
+// `out`, `stride` and `word` are the same in every lane.
+__device__ __forceinline__ void add_fresh_bits(uint32_t fresh, uint32_t* sizes, int64_t out, int32_t stride, int word,
+                                               int lane)
+{
+    if (!__any_sync(kFull, fresh)) return;
+    uint32_t mine = 0;
+    for (int b = 0; b < 32; ++b) {
+        const uint32_t c = __popc(__ballot_sync(kFull, (fresh >> b) & 1u));
+        if (lane == b) mine = c;
+    }
+    if (mine) atomicAdd(sizes + out + (int64_t)(word * 32 + lane) * stride, mine);
 }
 
 __global__ void k_segmask(int32_t n, int32_t nvl, int32_t segw, const int32_t* __restrict__ offsets,
@@ -501,6 +542,27 @@ __global__ void k_segmask(int32_t n, int32_t nvl, int32_t segw, const int32_t* _
     }
 }
 
+// Thread per entry: self-loop bits, and whether the entry's reverse exists.
+__global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const int32_t* __restrict__ offsets,
+                              const uint64_t* __restrict__ adj, const int32_t* __restrict__ vrank,
+                              uint32_t* __restrict__ selfloop, uint32_t* status)
+{
+    bool asym = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t ent = adj[i];
+        const uint32_t u = (uint32_t)src[i], x = entry_to(ent);
+        if (u == x) {
+            atomicOr(selfloop + (u >> 5), 1u << (u & 31));
+            continue;
+        }
+        const uint64_t rk = pack_entry(entry_el(ent), (uint32_t)vrank[u], u);
+        const int32_t b = offsets[x], e = offsets[x + 1];
+        const int32_t p = lower_bound_entry(adj, b, e, rk);
+        asym |= p >= e || adj[p] != rk;
+    }
+    if (__any_sync(kFull, asym) && (threadIdx.x & 31) == 0) atomicOr(status, kErrAsymmetric);
+}
+
 __device__ __forceinline__ int32_t find_parent_tile(const ParentMeta* parents, int32_t np, long long tile)
 {
     int32_t lo = 0, hi = np - 1;
@@ -511,9 +573,10 @@ __device__ __forceinline__ int32_t find_parent_tile(const ParentMeta* parents, i
     return lo;
 }
 
-// Row pass: lane per row.  Updates R, H and M for every source, and counts and
-// MB masks for backward tuples (at most one per row and rightmost-path target).
-__global__ void __launch_bounds__(kMaskWarps * 32) k_mask_rows(MaskDev a)
+// Row pass: lane per row.  Updates R (listing new source images), H and M for
+// every source, and counts and MB masks for backward tuples (at most one per
+// row and rightmost-path target).
+__global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
 {
     __shared__ int32_t img_s[kMaskWarps][32][kMaxV + 1];
     int32_t (*img_all)[kMaxV + 1] = img_s[threadIdx.x >> 5];
@@ -537,11 +600,29 @@ __global__ void __launch_bounds__(kMaskWarps * 32) k_mask_rows(MaskDev a)
         for (int s = 0; s < nsrc; ++s) {
             const int32_t u = live ? img[P.src_v[s]] : -1;
             const unsigned lm = __ballot_sync(kFull, live);
+            bool first_row = false;   // this lane's group made R[u] non-zero
             if (live) {
                 const unsigned peers = __match_any_sync(lm, u);
-                if (lane == __ffs(peers) - 1) atomicAdd(a.R + P.r_off + (int64_t)s * a.n + u, (uint32_t)__popc(peers));
+                if (lane == __ffs(peers) - 1)
+                    first_row = atomicAdd(a.R + P.r_off + (int64_t)s * a.n + u, (uint32_t)__popc(peers)) == 0;
             }
-            if (!live) continue;
+            // One append per warp for the source images seen for the first time.
+            const unsigned fm = __ballot_sync(kFull, first_row);
+            if (fm) {
+                const int first = __ffs(fm) - 1;
+                uint32_t base = 0;
+                if (lane == first) base = atomicAdd(a.tcount + P.ps_begin + s, (uint32_t)__popc(fm));
+                base = __shfl_sync(kFull, base, first);
+                if (first_row) {
+                    const uint32_t slot = base + __popc(fm & lanemask_lt());
+                    if (slot < (uint32_t)P.t_cap)
+                        a.touched[P.t_off + (int64_t)s * P.t_cap + slot] = u;
+                    else
+                        atomicOr(a.status, kErrCursor);
+                }
+            }
+            uint32_t mk[kMaxMaskWords] = {0, 0, 0, 0};
+            if (live) {
             const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
             const uint64_t lo = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
                                        : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
@@ -562,6 +643,20 @@ __global__ void __launch_bounds__(kMaskWarps * 32) k_mask_rows(MaskDev a)
                         bool dup = false;
                         for (int q = i; q < j; ++q) dup |= img[q] == x;
                         if (dup) continue;
+                        // Most image pairs are not adjacent.  A vertex reaches
+                        // itself only through a self-loop; a pair that the
+                        // pattern does not join is first looked up from the
+                        // shorter side when the graph is symmetric.
+                        if (x == u) {
+                            if (!((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
+                        } else if (a.symmetric && !((P.src_adj[s] >> j) & 1)) {
+                            const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
+                            if (4 * (xe - xb) < e - b) {
+                                const uint64_t rk = pack_entry((uint32_t)el, (uint32_t)P.vlab[P.src_v[s]], (uint32_t)u);
+                                const int32_t rp = lower_bound_entry(a.adj, xb, xe, rk);
+                                if (rp >= xe || __ldg(a.adj + rp) != rk) continue;
+                            }
+                        }
                         const uint64_t key = seg0 | (uint32_t)x;
                         const int32_t lb = lower_bound_entry(a.adj, b, e, key);
                         int32_t ub = lb;
@@ -589,15 +684,14 @@ __global__ void __launch_bounds__(kMaskWarps * 32) k_mask_rows(MaskDev a)
                     }
                 }
             }
-            uint32_t mk[kMaxMaskWords];
 #pragma unroll
             for (int w = 0; w < kMaxMaskWords; ++w)
                 mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
+            }
             for (int p = 0; p < nv; ++p) {
-                uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * a.n + img[p]) * mw;
-#pragma unroll
-                for (int w = 0; w < kMaxMaskWords; ++w)
-                    if (w < mw) or_words(rowm + w, mk[w]);
+                uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * a.n + (live ? img[p] : 0)) * mw;
+                const int64_t out = P.sz_off + (int64_t)s * K * (nv + 1) + p;
+                for (int w = 0; w < mw; ++w) add_fresh_bits(or_fresh(rowm + w, mk[w]), a.sizes, out, nv + 1, w, lane);
             }
         }
 
@@ -633,16 +727,37 @@ __global__ void __launch_bounds__(kMaskWarps * 32) k_mask_rows(MaskDev a)
             if (ok) {
                 const unsigned peers = __match_any_sync(mask, key);
                 if (lane == __ffs(peers) - 1) atomicAdd(a.counts + key, (unsigned long long)__popc(peers));
-                for (int p = 0; p < nv; ++p)
-                    or_words(a.MB + P.b_off + ((int64_t)p * a.n + img[p]) * P.bw + (bk >> 5), 1u << (bk & 31));
+            }
+            if (mask) {
+                const int64_t out = P.sz_off + (int64_t)nsrc * K * (nv + 1);
+                for (int p = 0; p < nv; ++p) {
+                    const uint32_t got =
+                        ok ? or_fresh(a.MB + P.b_off + ((int64_t)p * a.n + img[p]) * P.bw + (bk >> 5), 1u << (bk & 31))
+                           : 0u;
+                    for (int w = 0; w < P.bw; ++w)
+                        add_fresh_bits((bk >> 5) == w ? got : 0u, a.sizes, out + p, nv, w, lane);
+                }
             }
         }
         __syncwarp();
     }
 }
 
-// Sweep: warp per (parent, source, vertex u with R[u] > 0) over u's entries in
-// the source's range: child counts by tuple and the new vertex's domain masks.
+// Exclusive prefix of the touched-list lengths: the sweep's task numbering.
+__global__ void k_mask_prefix(int32_t nps, const uint32_t* __restrict__ tcount, unsigned long long* __restrict__ tprefix)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned long long run = 0;
+    for (int32_t i = 0; i < nps; ++i) {
+        tprefix[i] = run;
+        run += tcount[i];
+    }
+    tprefix[nps] = run;
+}
+
+// Sweep: warp per touched (parent, source, vertex u) over u's entries in the
+// source's range: child counts by tuple and the new vertex's domain masks.
+// R[u] and the H entries it reads are reset to zero.
 __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
 {
     const int lane = threadIdx.x & 31;
@@ -650,26 +765,30 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int32_t K = a.nel * a.nvl;
     const int mw = a.mw;
+    const unsigned long long total = a.tprefix[a.nps];
     unsigned long long scanned = 0;
-    for (int64_t task = warp; task < a.nsweep; task += nwarps) {
-        int32_t lo = 0, hi = a.nparents - 1;
+    for (unsigned long long task = warp; task < total; task += nwarps) {
+        int32_t lo = 0, hi = a.nps - 1;
         while (lo < hi) {
             const int32_t mid = (lo + hi + 1) >> 1;
-            if (a.parents[mid].sweep_begin <= task) lo = mid; else hi = mid - 1;
+            if (a.tprefix[mid] <= task) lo = mid; else hi = mid - 1;
         }
-        const ParentMeta& P = a.parents[lo];
-        const int64_t local = task - P.sweep_begin;
-        const int s = (int)(local / a.n);
-        const int32_t u = (int32_t)(local % a.n);
-        const uint32_t r = __ldg(a.R + P.r_off + (int64_t)s * a.n + u);
-        if (r == 0) continue;
+        const ParentMeta& P = a.parents[a.ps_parent[lo]];
+        const int s = lo - P.ps_begin;
+        const int64_t idx = (int64_t)(task - a.tprefix[lo]);
+        if (idx >= P.t_cap) continue;   // the row pass flagged an overflow; never read past the list
+        const int32_t u = a.touched[P.t_off + (int64_t)s * P.t_cap + idx];
+        uint32_t* Ru = a.R + P.r_off + (int64_t)s * a.n + u;
+        const uint32_t r = *Ru;
+        __syncwarp();
         const int min_label = P.min_label;
         const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
         const uint64_t lo_key = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
                                        : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
         const int32_t st = lower_bound_entry(a.adj, b, e, lo_key);
-        const uint32_t* Hs = a.H + P.h_off + (int64_t)s * a.m;
+        uint32_t* Hs = a.H + P.h_off + (int64_t)s * a.m;
         uint32_t* NM = a.M + P.m_off + ((int64_t)s * (P.nv + 1) + P.nv) * a.n * mw;
+        const int64_t nm_out = P.sz_off + (int64_t)s * K * (P.nv + 1) + P.nv;
         unsigned long long* cnt = a.counts + P.key_base + (int64_t)s * K;
         scanned += (unsigned long long)(e - st);
         for (int32_t base = st; base < e; base += 32) {
@@ -683,7 +802,9 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
                 ok = tl >= min_label;
                 kc = (int32_t)entry_el(ent) * a.nvl + tl;
                 to = entry_to(ent);
-                diff = r - __ldg(Hs + i);
+                const uint32_t h = Hs[i];
+                if (h) Hs[i] = 0u;
+                diff = r - h;
             }
             // Entries are sorted by tuple, so equal tuples sit in adjacent lanes.
             const int32_t segk = ok ? kc : (int32_t)(0x40000000 + lane);
@@ -696,43 +817,19 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
             }
             const int32_t nk = __shfl_down_sync(kFull, segk, 1);
             if (ok && (lane == 31 || nk != segk) && v) atomicAdd(cnt + kc, v);
-            if (ok && diff > 0) or_words(NM + (int64_t)to * mw + (kc >> 5), 1u << (kc & 31));
+            const bool fresh = ok && diff > 0 && or_fresh(NM + (int64_t)to * mw + (kc >> 5), 1u << (kc & 31));
+            const unsigned fmask = __ballot_sync(kFull, fresh);
+            if (fresh) {
+                const unsigned peers = __match_any_sync(fmask, kc);
+                if (lane == __ffs(peers) - 1)
+                    atomicAdd(a.sizes + nm_out + (int64_t)kc * (P.nv + 1), (uint32_t)__popc(peers));
+            }
         }
+        __syncwarp();
+        if (lane == 0) *Ru = 0u;
     }
     scanned += __shfl_xor_sync(kFull, scanned, 16);
     if (lane == 0 && scanned) atomicAdd(a.scanned, scanned);
-}
-
-// Column popcounts of key-mask matrices: block row y = matrix, x-blocks split
-// the vertices; lane b of a warp accumulates bit b of each word.
-__global__ void __launch_bounds__(256) k_mask_sizes(const MaskMatrix* __restrict__ mats, const uint32_t* __restrict__ M,
-                                                    const uint32_t* __restrict__ MB, int32_t n,
-                                                    uint32_t* __restrict__ sizes)
-{
-    const MaskMatrix mm = mats[blockIdx.y];
-    const uint32_t* base = (mm.in_mb ? MB : M) + mm.base;
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    uint32_t acc[kMaxMaskWords] = {0, 0, 0, 0};
-    for (int64_t x0 = warp * 32; x0 < n; x0 += nwarps * 32) {
-        const int64_t x = x0 + lane;
-#pragma unroll
-        for (int w = 0; w < kMaxMaskWords; ++w) {
-            if (w >= mm.width) break;
-            const uint32_t val = x < n ? __ldcs(base + x * mm.width + w) : 0u;
-            if (!__any_sync(kFull, val)) continue;
-            for (int bit = 0; bit < 32; ++bit) {
-                const uint32_t c = __popc(__ballot_sync(kFull, (val >> bit) & 1u));
-                if (lane == bit) acc[w] += c;
-            }
-        }
-    }
-#pragma unroll
-    for (int w = 0; w < kMaxMaskWords; ++w) {
-        const int32_t kc = w * 32 + lane;
-        if (w < mm.width && kc < mm.nbits && acc[w]) atomicAdd(sizes + mm.out + (int64_t)kc * mm.stride, acc[w]);
-    }
 }
 
 // Block per (active tuple, pattern vertex): the size of that domain.
@@ -853,6 +950,13 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     return cudaGetLastError();
 }
 
+cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st)
+{
+    if (g.m == 0) return cudaSuccess;
+    k_graph_flags<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj, g.vrank, g.selfloop, status);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_segmask(DevGraph& g, cudaStream_t st)
 {
     if (g.n == 0 || g.segw == 0) return cudaSuccess;
@@ -867,6 +971,8 @@ MaskDev mask_dev(const MaskArgs& x)
     a.offsets = x.g->offsets;
     a.adj = x.g->adj;
     a.segmask = x.g->segmask;
+    a.selfloop = x.g->selfloop;
+    a.symmetric = x.g->symmetric;
     a.n = x.g->n;
     a.m = x.g->m;
     a.nvl = x.g->nvl;
@@ -875,13 +981,18 @@ MaskDev mask_dev(const MaskArgs& x)
     a.parents = x.parents;
     a.nparents = x.nparents;
     a.ntiles = x.ntiles;
-    a.nsweep = x.nsweep;
     a.in_cols = x.in_col_ptrs;
     a.counts = x.counts;
+    a.sizes = x.sizes;
     a.R = x.R;
     a.H = x.H;
     a.M = x.M;
     a.MB = x.MB;
+    a.touched = x.touched;
+    a.tcount = x.tcount;
+    a.ps_parent = x.ps_parent;
+    a.nps = x.nps;
+    a.tprefix = x.tprefix;
     a.tile_counter = x.tile_counter;
     a.scanned = x.scanned;
     a.status = x.status;
@@ -908,21 +1019,9 @@ cudaError_t launch_mask_rows(const MaskArgs& x, cudaStream_t st)
 
 cudaError_t launch_mask_sweep(const MaskArgs& x, cudaStream_t st)
 {
-    if (x.nsweep == 0) return cudaSuccess;
-    const int64_t need = (x.nsweep + 7) / 8;
-    const int64_t cap = (int64_t)sm_count() * 8;
-    k_mask_sweep<<<(int)(need < cap ? need : cap), 256, 0, st>>>(mask_dev(x));
-    return cudaGetLastError();
-}
-
-cudaError_t launch_mask_sizes(const MaskMatrix* mats, int32_t nmats, const uint32_t* M, const uint32_t* MB,
-                              int32_t n, uint32_t* sizes, cudaStream_t st)
-{
-    const int xblocks = (int)std::min<int64_t>(64, ((int64_t)n + 255) / 256);
-    for (int32_t first = 0; first < nmats; first += 65535) {
-        const int32_t cnt = std::min<int32_t>(65535, nmats - first);
-        k_mask_sizes<<<dim3(xblocks < 1 ? 1 : xblocks, cnt), 256, 0, st>>>(mats + first, M, MB, n, sizes);
-    }
+    if (x.nps == 0) return cudaSuccess;
+    k_mask_prefix<<<1, 32, 0, st>>>(x.nps, x.tcount, x.tprefix);
+    k_mask_sweep<<<sm_count() * 8, 256, 0, st>>>(mask_dev(x));
     return cudaGetLastError();
 }
 

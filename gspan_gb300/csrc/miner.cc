@@ -436,12 +436,21 @@ struct Run {
                 if (e.from < e.to) P.vlab[e.to] = (int16_t)e.tl;
             P.nsrc = (int16_t)(rm.size() + 1);
             P.src_v[0] = P.vn;
+            auto joined = [&](int v) {
+                uint16_t bits = 0;
+                for (const CodeEdge& e : c) {
+                    if (e.from == v) bits |= (uint16_t)(1u << e.to);
+                    if (e.to == v) bits |= (uint16_t)(1u << e.from);
+                }
+                return bits;
+            };
             for (size_t s2 = 1; s2 <= rm.size(); ++s2) {
                 const CodeEdge& e = c[rm[s2 - 1]];
                 P.src_v[s2] = (int16_t)e.from;
                 P.src_el[s2] = (int16_t)e.el;
                 P.src_tl[s2] = P.vlab[e.to];
             }
+            for (int s2 = 0; s2 < P.nsrc; ++s2) P.src_adj[s2] = joined(P.src_v[s2]);
             P.nback = (int16_t)(rm.size() - 1);
             for (int t = 0; t < P.nback; ++t) {
                 const CodeEdge& e = c[rm[t + 1]];
@@ -477,68 +486,88 @@ struct Run {
             }
             if (mask_possible && P.bw <= kMaxMaskWords) {
                 const int64_t rows = P.row_end - P.row_begin;
-                const double dense = (double)P.nsrc * ((double)g.n + g.m) +
-                                     (double)P.nsrc * (nv + 1) * g.n * g.segw + (double)nv * g.n * P.bw;
-                use_mask[i] = mode == 2 || (double)rows * P.nsrc * g.edge_biased_degree > 2.0 * dense;
+                // The mask path clears M and MB per parent (R and H are left
+                // zero by its sweep); the per-candidate path examines about
+                // rows x sources x (mean degree behind an embedding's vertex)
+                // candidates, each far dearer than clearing a word.
+                const double clear_words = (double)P.nsrc * (nv + 1) * g.n * g.segw + (double)nv * g.n * P.bw;
+                use_mask[i] = mode == 2 || (double)rows * P.nsrc * g.edge_biased_degree > 0.125 * clear_words;
             }
         }
 
-        // Groups: mask-path parents, per-candidate parents, and all (materialisation).
-        std::vector<ParentMeta> mg, cg, all = meta;
+        // Mask-path parents run in groups whose arrays fit a memory budget;
+        // per-candidate parents in one launch; all parents for materialisation.
+        struct MGroup {
+            std::vector<ParentMeta> metas;
+            std::vector<int32_t> ps_parent;
+            int64_t tiles = 0, r = 0, h = 0, m = 0, b = 0, t = 0;
+            double bytes = 0;
+        };
+        std::vector<MGroup> groups;
+        std::vector<ParentMeta> cg, all = meta;
         std::vector<int64_t> sz_off(np, -1);
-        int64_t mtiles = 0, ctiles = 0, atiles = 0, nsweep = 0;
-        int64_t r_words = 0, h_words = 0, m_words = 0, b_words = 0, sz_total = 0;
-        std::vector<MaskMatrix> mats;
+        int64_t ctiles = 0, atiles = 0, sz_total = 0;
         double rows_bytes = 0, cand_read_bytes = 0, all_read_bytes = 0;
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        const double budget = std::max(2.0e9, 0.4 * (double)free_b);
         for (int i = 0; i < np; ++i) {
             ParentMeta& A = all[i];
             const int64_t rows = A.row_end - A.row_begin;
             A.tile_begin = atiles;
             atiles += (rows + 31) / 32;
             all_read_bytes += (double)rows * (4.0 * A.nv + 8.0 * A.nsrc);
-            if (use_mask[i]) {
-                ParentMeta P = meta[i];
-                P.tile_begin = mtiles;
-                mtiles += (rows + 31) / 32;
-                P.sweep_begin = nsweep;
-                nsweep += (int64_t)P.nsrc * g.n;
-                P.r_off = r_words;
-                r_words += (int64_t)P.nsrc * g.n;
-                P.h_off = h_words;
-                h_words += (int64_t)P.nsrc * g.m;
-                P.m_off = m_words;
-                m_words += (int64_t)P.nsrc * (P.nv + 1) * g.n * g.segw;
-                P.b_off = b_words;
-                b_words += (int64_t)P.nv * g.n * P.bw;
-                sz_off[i] = sz_total;
-                for (int s2 = 0; s2 < P.nsrc; ++s2)
-                    for (int p = 0; p <= P.nv; ++p)
-                        mats.push_back(MaskMatrix{P.m_off + ((int64_t)s2 * (P.nv + 1) + p) * g.n * g.segw,
-                                                  sz_total + (int64_t)s2 * K * (P.nv + 1) + p, g.segw, K, P.nv + 1, 0});
-                if (P.nback > 0)
-                    for (int p = 0; p < P.nv; ++p)
-                        mats.push_back(MaskMatrix{P.b_off + (int64_t)p * g.n * P.bw,
-                                                  sz_total + (int64_t)P.nsrc * K * (P.nv + 1) + p, P.bw,
-                                                  P.nback * g.nel, P.nv, 1});
-                sz_total += (int64_t)P.nsrc * K * (P.nv + 1) + (int64_t)P.nback * g.nel * P.nv;
-                rows_bytes += (double)rows * (4.0 * P.nv + P.nsrc * (16.0 + 4.0 * g.segw + 4.0 * P.nv * g.segw) +
-                                              8.0 * P.nback);
-                mg.push_back(P);
-            } else {
+            if (!use_mask[i]) {
                 ParentMeta P = meta[i];
                 P.tile_begin = ctiles;
                 ctiles += (rows + 31) / 32;
                 cand_read_bytes += (double)rows * (4.0 * P.nv + 8.0 * P.nsrc);
                 cg.push_back(P);
+                continue;
             }
+            ParentMeta P = meta[i];
+            const int64_t t_cap = std::min<int64_t>(rows, g.n);
+            const int64_t rw = (int64_t)P.nsrc * g.n, hw = (int64_t)P.nsrc * g.m;
+            const int64_t mw2 = (int64_t)P.nsrc * (P.nv + 1) * g.n * g.segw, bw2 = (int64_t)P.nv * g.n * P.bw;
+            const int64_t tw = (int64_t)P.nsrc * t_cap;
+            const double bytes = 4.0 * (double)(rw + hw + mw2 + bw2 + tw);
+            if (groups.empty() || (!groups.back().metas.empty() && groups.back().bytes + bytes > budget))
+                groups.emplace_back();
+            MGroup& G = groups.back();
+            P.tile_begin = G.tiles;
+            G.tiles += (rows + 31) / 32;
+            P.r_off = G.r;
+            G.r += rw;
+            P.h_off = G.h;
+            G.h += hw;
+            P.m_off = G.m;
+            G.m += mw2;
+            P.b_off = G.b;
+            G.b += bw2;
+            P.t_off = G.t;
+            G.t += tw;
+            P.t_cap = (int32_t)t_cap;
+            P.ps_begin = (int32_t)G.ps_parent.size();
+            for (int s2 = 0; s2 < P.nsrc; ++s2) G.ps_parent.push_back((int32_t)G.metas.size());
+            P.sz_off = sz_total;
+            sz_off[i] = sz_total;
+            sz_total += (int64_t)P.nsrc * K * (P.nv + 1) + (int64_t)P.nback * g.nel * P.nv;
+            G.bytes += bytes;
+            rows_bytes += (double)rows * (4.0 * P.nv + P.nsrc * (16.0 + 4.0 * g.segw + 4.0 * P.nv * g.segw) +
+                                          8.0 * P.nback);
+            G.metas.push_back(P);
         }
-        st.mask_parents += mg.size();
+        size_t nmask = 0;
+        for (const MGroup& G : groups) nmask += G.metas.size();
+        st.mask_parents += nmask;
         st.candidate_parents += cg.size();
 
         unsigned long long* d_counts = nullptr;
         ParentMeta *d_mg = nullptr, *d_cg = nullptr, *d_all = nullptr;
         uint32_t *d_R = nullptr, *d_H = nullptr, *d_M = nullptr, *d_MB = nullptr, *d_sizes = nullptr;
-        MaskMatrix* d_mats = nullptr;
+        uint32_t* d_tcount = nullptr;
+        int32_t *d_touched = nullptr, *d_psp = nullptr;
+        unsigned long long* d_tprefix = nullptr;
         auto release = [&]() {
             dfree(d_counts, s);
             dfree(d_mg, s);
@@ -549,7 +578,10 @@ struct Run {
             dfree(d_M, s);
             dfree(d_MB, s);
             dfree(d_sizes, s);
-            dfree(d_mats, s);
+            dfree(d_tcount, s);
+            dfree(d_touched, s);
+            dfree(d_psp, s);
+            dfree(d_tprefix, s);
         };
         struct Guard {
             std::function<void()> f;
@@ -561,48 +593,68 @@ struct Run {
         GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), s), "clear counters");
 
         cudaEvent_t e0, e1;
-        if (!mg.empty()) {
-            GS_CK(dalloc(&d_mg, mg.size(), s), "alloc mask parents");
-            GS_CK(copy(d_mg, mg.data(), mg.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
-            GS_CK(dalloc(&d_R, (size_t)r_words, s), "alloc R");
-            GS_CK(dalloc(&d_H, (size_t)h_words, s), "alloc H");
-            GS_CK(dalloc(&d_M, (size_t)std::max<int64_t>(m_words, 1), s), "alloc M");
-            GS_CK(dalloc(&d_MB, (size_t)std::max<int64_t>(b_words, 1), s), "alloc MB");
+        if (!groups.empty()) {
+            int64_t mr = 0, mh = 0, mm = 0, mb = 0, mt = 0, mps = 0, mmeta = 0;
+            for (const MGroup& G : groups) {
+                mr = std::max(mr, G.r);
+                mh = std::max(mh, G.h);
+                mm = std::max(mm, G.m);
+                mb = std::max(mb, G.b);
+                mt = std::max(mt, G.t);
+                mps = std::max<int64_t>(mps, (int64_t)G.ps_parent.size());
+                mmeta = std::max<int64_t>(mmeta, (int64_t)G.metas.size());
+            }
+            GS_CK(dalloc(&d_R, (size_t)mr, s), "alloc R");
+            GS_CK(dalloc(&d_H, (size_t)std::max<int64_t>(mh, 1), s), "alloc H");
+            GS_CK(dalloc(&d_M, (size_t)std::max<int64_t>(mm, 1), s), "alloc M");
+            GS_CK(dalloc(&d_MB, (size_t)std::max<int64_t>(mb, 1), s), "alloc MB");
+            GS_CK(dalloc(&d_touched, (size_t)std::max<int64_t>(mt, 1), s), "alloc touched");
+            GS_CK(dalloc(&d_tcount, (size_t)mps, s), "alloc touched counts");
+            GS_CK(dalloc(&d_tprefix, (size_t)mps + 1, s), "alloc touched prefix");
+            GS_CK(dalloc(&d_psp, (size_t)mps, s), "alloc slot parents");
+            GS_CK(dalloc(&d_mg, (size_t)mmeta, s), "alloc mask parents");
             GS_CK(dalloc(&d_sizes, (size_t)std::max<int64_t>(sz_total, 1), s), "alloc sizes");
-            GS_CK(cudaMemsetAsync(d_R, 0, r_words * 4, s), "clear R");
-            GS_CK(cudaMemsetAsync(d_H, 0, h_words * 4, s), "clear H");
-            GS_CK(cudaMemsetAsync(d_M, 0, std::max<int64_t>(m_words, 1) * 4, s), "clear M");
-            GS_CK(cudaMemsetAsync(d_MB, 0, std::max<int64_t>(b_words, 1) * 4, s), "clear MB");
+            GS_CK(cudaMemsetAsync(d_R, 0, mr * 4, s), "clear R");
+            GS_CK(cudaMemsetAsync(d_H, 0, std::max<int64_t>(mh, 1) * 4, s), "clear H");
             GS_CK(cudaMemsetAsync(d_sizes, 0, std::max<int64_t>(sz_total, 1) * 4, s), "clear sizes");
-            GS_CK(dalloc(&d_mats, mats.size(), s), "alloc matrices");
-            GS_CK(copy(d_mats, mats.data(), mats.size() * sizeof(MaskMatrix), cudaMemcpyHostToDevice, s),
-                  "copy matrices");
-            MaskArgs ma{};
-            ma.g = &g;
-            ma.parents = d_mg;
-            ma.nparents = (int32_t)mg.size();
-            ma.ntiles = mtiles;
-            ma.nsweep = nsweep;
-            ma.in_col_ptrs = table.d_cols;
-            ma.counts = d_counts;
-            ma.R = d_R;
-            ma.H = d_H;
-            ma.M = d_M;
-            ma.MB = d_MB;
-            ma.tile_counter = ctx->d_counters + 2;
-            ma.scanned = ctx->d_counters + 3;
-            ma.status = ctx->d_status;
-            tic(&e0, &e1);
-            GS_CK(launch_mask_rows(ma, s), "mask row pass launch");
-            toc(e0, e1, &st.rows_ms);
-            tic(&e0, &e1);
-            GS_CK(launch_mask_sweep(ma, s), "mask sweep launch");
-            toc(e0, e1, &st.sweep_ms);
-            tic(&e0, &e1);
-            GS_CK(launch_mask_sizes(d_mats, (int32_t)mats.size(), d_M, d_MB, g.n, d_sizes, s), "mask sizes launch");
-            toc(e0, e1, &st.domain_ms);
-            st.kernel_launches += 3;
-            st.rows_launches += 1;
+            for (const MGroup& G : groups) {
+                GS_CK(copy(d_mg, G.metas.data(), G.metas.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s),
+                      "copy mask parents");
+                GS_CK(copy(d_psp, G.ps_parent.data(), G.ps_parent.size() * 4, cudaMemcpyHostToDevice, s),
+                      "copy slot parents");
+                if (G.m) GS_CK(cudaMemsetAsync(d_M, 0, G.m * 4, s), "clear M");
+                if (G.b) GS_CK(cudaMemsetAsync(d_MB, 0, G.b * 4, s), "clear MB");
+                GS_CK(cudaMemsetAsync(d_tcount, 0, G.ps_parent.size() * 4, s), "clear touched counts");
+                GS_CK(cudaMemsetAsync(ctx->d_counters + 2, 0, 8, s), "clear tile counter");
+                MaskArgs ma{};
+                ma.g = &g;
+                ma.parents = d_mg;
+                ma.nparents = (int32_t)G.metas.size();
+                ma.ntiles = G.tiles;
+                ma.in_col_ptrs = table.d_cols;
+                ma.counts = d_counts;
+                ma.sizes = d_sizes;
+                ma.R = d_R;
+                ma.H = d_H;
+                ma.M = d_M;
+                ma.MB = d_MB;
+                ma.touched = d_touched;
+                ma.tcount = d_tcount;
+                ma.ps_parent = d_psp;
+                ma.nps = (int32_t)G.ps_parent.size();
+                ma.tprefix = d_tprefix;
+                ma.tile_counter = ctx->d_counters + 2;
+                ma.scanned = ctx->d_counters + 3;
+                ma.status = ctx->d_status;
+                tic(&e0, &e1);
+                GS_CK(launch_mask_rows(ma, s), "mask row pass launch");
+                toc(e0, e1, &st.rows_ms);
+                tic(&e0, &e1);
+                GS_CK(launch_mask_sweep(ma, s), "mask sweep launch");
+                toc(e0, e1, &st.sweep_ms);
+                st.kernel_launches += 3;
+                st.rows_launches += 1;
+            }
             st.rows_bytes += rows_bytes;
         }
         ExpandArgs x{};
@@ -635,12 +687,17 @@ struct Run {
         resolve();
         st.scanned_entries += ctr[1] + ctr[3];
         if (!cg.empty()) st.expand_bytes += cand_read_bytes + 8.0 * (double)ctr[1];
-        if (!mg.empty()) st.sweep_bytes += 12.0 * (double)ctr[3] + 4.0 * (double)r_words;
-        // The mask kernels are done with R, H and M.
+        if (!groups.empty()) st.sweep_bytes += 12.0 * (double)ctr[3];
+        uint32_t mstat = 0;
+        GS_CK(copy(&mstat, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
+        GS_CK(cudaStreamSynchronize(s), "read status");
+        if (mstat) return fail(ctx, GSPAN_ERR_DEVICE, "kernel status word " + std::to_string(mstat));
+        // The mask kernels are done with their arrays.
         dfree(d_R, s);
         dfree(d_H, s);
         dfree(d_M, s);
         dfree(d_MB, s);
+        dfree(d_touched, s);
 
         // Which children count: enough embeddings, minimum code, and (mask
         // path) support from the domain sizes.
@@ -754,6 +811,31 @@ struct Run {
         GS_CK(dalloc(&out.d_cols, (size_t)ncols, s), "alloc column table");
         GS_CK(copy(out.d_cols, out.cols.data(), ncols * sizeof(int32_t*), cudaMemcpyHostToDevice, s),
               "copy column table");
+        // Per parent, the frequent forward tuples to scan segment by segment.
+        {
+            std::vector<std::vector<std::pair<int16_t, uint32_t>>> segs_of(np);
+            std::vector<int> key_parent;
+            for (const Freq& f : freq) {
+                int i = (int)(std::upper_bound(meta.begin(), meta.end(), f.key,
+                                               [](int32_t k2, const ParentMeta& m2) { return k2 < m2.key_base; }) -
+                              meta.begin()) - 1;
+                const int64_t lk = f.key - meta[i].key_base;
+                if (lk < (int64_t)meta[i].nsrc * K)
+                    segs_of[i].emplace_back((int16_t)(lk / K), (uint32_t)(lk % K));
+            }
+            for (int i = 0; i < np; ++i) {
+                ParentMeta& A = all[i];
+                if ((int)segs_of[i].size() > kMaxV) {
+                    A.nmseg = -1;
+                    continue;
+                }
+                A.nmseg = (int16_t)segs_of[i].size();
+                for (size_t q = 0; q < segs_of[i].size(); ++q) {
+                    A.mseg_s[q] = segs_of[i][q].first;
+                    A.mseg_kc[q] = segs_of[i][q].second;
+                }
+            }
+        }
         GS_CK(dalloc(&d_all, all.size(), s), "alloc parents");
         GS_CK(copy(d_all, all.data(), all.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
         GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 16, s), "clear counters");
