@@ -195,9 +195,110 @@ gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t n, int32_t m, const int3
     g.n = n;
     g.m = m;
 
-    std::vector<int32_t> vrank;
-    rank_labels(vlabels, (size_t)n, 1, g.vlabel_of_rank, &vrank);
-    rank_labels(m > 0 ? &edges[0].label : nullptr, (size_t)m, 3, g.elabel_of_rank, nullptr);
+    // Temporaries of the build, freed on every path.
+    gspan_edge* d_edges = nullptr;
+    int32_t *d_vl = nullptr, *d_minmax = nullptr, *d_vtab = nullptr, *d_etab = nullptr, *d_elabels = nullptr;
+    uint8_t *d_vflag = nullptr, *d_eflag = nullptr;
+    uint64_t* d_tmp = nullptr;
+    auto cleanup = [&]() {
+        for (void* p : {(void*)d_edges, (void*)d_vl, (void*)d_minmax, (void*)d_vtab, (void*)d_etab, (void*)d_elabels,
+                        (void*)d_vflag, (void*)d_eflag, (void*)d_tmp})
+            if (p) cudaFreeAsync(p, s);
+        d_edges = nullptr;
+        d_vl = d_minmax = d_vtab = d_etab = d_elabels = nullptr;
+        d_vflag = d_eflag = nullptr;
+        d_tmp = nullptr;
+    };
+    auto drop = [&]() {
+        cleanup();
+        free_graph(gr, s);
+        cudaStreamSynchronize(s);
+        delete gr;
+    };
+    auto bail = [&](cudaError_t e, const char* what) {
+        drop();
+        return cuda_fail(ctx, e, what);
+    };
+    cudaError_t e;
+#define UP_CK(call, what) \
+    if ((e = (call)) != cudaSuccess) return bail(e, what)
+    UP_CK(cudaMallocAsync(&g.offsets, ((size_t)n + 1) * 4, s), "alloc offsets");
+    UP_CK(cudaMemcpyAsync(g.offsets, offsets, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice, s), "copy offsets");
+    if (n > 0) {
+        UP_CK(cudaMallocAsync(&d_vl, (size_t)n * 4, s), "alloc labels");
+        UP_CK(cudaMemcpyAsync(d_vl, vlabels, (size_t)n * 4, cudaMemcpyHostToDevice, s), "copy labels");
+        UP_CK(cudaMallocAsync(&g.vrank, (size_t)n * 4, s), "alloc vrank");
+    }
+    if (m > 0) {
+        UP_CK(cudaMallocAsync(&d_edges, (size_t)m * sizeof(gspan_edge), s), "alloc edges");
+        UP_CK(cudaMemcpyAsync(d_edges, edges, (size_t)m * sizeof(gspan_edge), cudaMemcpyHostToDevice, s),
+              "copy edges");
+    }
+
+    // Label ranks: min/max and presence on the device, rank tables on the host
+    // (O(label range)); sparse ranges beyond 2^24 values rank on the host.
+    constexpr int64_t kDenseRange = (int64_t)1 << 24;
+    int32_t mm[4] = {INT32_MAX, INT32_MIN, INT32_MAX, INT32_MIN};
+    UP_CK(cudaMallocAsync(&d_minmax, sizeof(mm), s), "alloc minmax");
+    UP_CK(cudaMemcpyAsync(d_minmax, mm, sizeof(mm), cudaMemcpyHostToDevice, s), "init minmax");
+    if (n > 0 || m > 0) UP_CK(gs::launch_label_minmax(n, d_vl, m, d_edges, d_minmax, s), "label minmax launch");
+    UP_CK(cudaMemcpyAsync(mm, d_minmax, sizeof(mm), cudaMemcpyDeviceToHost, s), "read minmax");
+    UP_CK(cudaStreamSynchronize(s), "label minmax");
+    const int64_t vrange = n > 0 ? (int64_t)mm[1] - mm[0] + 1 : 0;
+    const int64_t erange = m > 0 ? (int64_t)mm[3] - mm[2] + 1 : 0;
+    int32_t elo = mm[2];
+    if (vrange <= kDenseRange && erange <= kDenseRange) {
+        std::vector<uint8_t> vflag((size_t)vrange), eflag((size_t)erange);
+        if (vrange) UP_CK(cudaMallocAsync(&d_vflag, (size_t)vrange, s), "alloc flags");
+        if (erange) UP_CK(cudaMallocAsync(&d_eflag, (size_t)erange, s), "alloc flags");
+        if (vrange) UP_CK(cudaMemsetAsync(d_vflag, 0, (size_t)vrange, s), "clear flags");
+        if (erange) UP_CK(cudaMemsetAsync(d_eflag, 0, (size_t)erange, s), "clear flags");
+        UP_CK(gs::launch_label_presence(n, d_vl, mm[0], d_vflag, m, d_edges, elo, d_eflag, s), "presence launch");
+        if (vrange) UP_CK(cudaMemcpyAsync(vflag.data(), d_vflag, (size_t)vrange, cudaMemcpyDeviceToHost, s), "flags");
+        if (erange) UP_CK(cudaMemcpyAsync(eflag.data(), d_eflag, (size_t)erange, cudaMemcpyDeviceToHost, s), "flags");
+        UP_CK(cudaStreamSynchronize(s), "label presence");
+        std::vector<int32_t> vtab((size_t)vrange, -1), etab((size_t)erange, -1);
+        for (int64_t v = 0; v < vrange; ++v)
+            if (vflag[(size_t)v]) {
+                vtab[(size_t)v] = (int32_t)g.vlabel_of_rank.size();
+                g.vlabel_of_rank.push_back((int32_t)(v + mm[0]));
+            }
+        for (int64_t v = 0; v < erange; ++v)
+            if (eflag[(size_t)v]) {
+                etab[(size_t)v] = (int32_t)g.elabel_of_rank.size();
+                g.elabel_of_rank.push_back((int32_t)(v + elo));
+            }
+        if (vrange) {
+            UP_CK(cudaMallocAsync(&d_vtab, (size_t)vrange * 4, s), "alloc rank table");
+            UP_CK(cudaMemcpyAsync(d_vtab, vtab.data(), (size_t)vrange * 4, cudaMemcpyHostToDevice, s), "rank table");
+            UP_CK(gs::launch_vertex_ranks(n, d_vl, mm[0], d_vtab, g.vrank, s), "vertex ranks launch");
+        }
+        if (erange) {
+            UP_CK(cudaMallocAsync(&d_etab, (size_t)erange * 4, s), "alloc rank table");
+            UP_CK(cudaMemcpyAsync(d_etab, etab.data(), (size_t)erange * 4, cudaMemcpyHostToDevice, s), "rank table");
+        }
+        UP_CK(cudaStreamSynchronize(s), "rank tables");   // host tables leave scope
+    } else {
+        std::vector<int32_t> vrank;
+        rank_labels(vlabels, (size_t)n, 1, g.vlabel_of_rank, &vrank);
+        rank_labels(m > 0 ? &edges[0].label : nullptr, (size_t)m, 3, g.elabel_of_rank, nullptr);
+        if (n > 0)
+            UP_CK(cudaMemcpyAsync(g.vrank, vrank.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s), "copy vrank");
+        if (!g.elabel_of_rank.empty()) {
+            UP_CK(cudaMallocAsync(&d_elabels, g.elabel_of_rank.size() * 4, s), "alloc edge labels");
+            UP_CK(cudaMemcpyAsync(d_elabels, g.elabel_of_rank.data(), g.elabel_of_rank.size() * 4,
+                                  cudaMemcpyHostToDevice, s),
+                  "copy edge labels");
+        }
+        UP_CK(cudaStreamSynchronize(s), "host ranks");
+    }
+    g.nvl = (int32_t)g.vlabel_of_rank.size();
+    g.nel = (int32_t)g.elabel_of_rank.size();
+    if (g.nvl > 0xFFFF || g.nel > 0xFFFF) {
+        drop();
+        return fail(ctx, GSPAN_ERR_LIMIT, "more than 65535 distinct vertex or edge labels");
+    }
+    // Mean degree behind an edge, for the kernel-path choice.
     {
         double d1 = 0, d2 = 0;
         for (int32_t v = 0; v < n; ++v) {
@@ -207,50 +308,14 @@ gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t n, int32_t m, const int3
         }
         g.edge_biased_degree = d1 > 0 ? d2 / d1 : 0.0;
     }
-    g.nvl = (int32_t)g.vlabel_of_rank.size();
-    g.nel = (int32_t)g.elabel_of_rank.size();
-    if (g.nvl > 0xFFFF || g.nel > 0xFFFF) {
-        delete gr;
-        return fail(ctx, GSPAN_ERR_LIMIT, "more than 65535 distinct vertex or edge labels");
-    }
 
-    gspan_edge* d_edges = nullptr;
-    int32_t* d_elabels = nullptr;
-    uint64_t* d_tmp = nullptr;
-    auto cleanup = [&]() {
-        if (d_edges) cudaFreeAsync(d_edges, s);
-        if (d_elabels) cudaFreeAsync(d_elabels, s);
-        if (d_tmp) cudaFreeAsync(d_tmp, s);
-    };
-    auto bail = [&](cudaError_t e, const char* what) {
-        cleanup();
-        free_graph(gr, s);
-        cudaStreamSynchronize(s);
-        delete gr;
-        return cuda_fail(ctx, e, what);
-    };
-    cudaError_t e;
-#define UP_CK(call, what) \
-    if ((e = (call)) != cudaSuccess) return bail(e, what)
-    UP_CK(cudaMallocAsync(&g.offsets, ((size_t)n + 1) * 4, s), "alloc offsets");
-    UP_CK(cudaMemcpyAsync(g.offsets, offsets, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice, s), "copy offsets");
-    if (n > 0) {
-        UP_CK(cudaMallocAsync(&g.vrank, (size_t)n * 4, s), "alloc vrank");
-        UP_CK(cudaMemcpyAsync(g.vrank, vrank.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s), "copy vrank");
-    }
     if (m > 0) {
-        UP_CK(cudaMallocAsync(&d_edges, (size_t)m * sizeof(gspan_edge), s), "alloc edges");
-        UP_CK(cudaMemcpyAsync(d_edges, edges, (size_t)m * sizeof(gspan_edge), cudaMemcpyHostToDevice, s),
-              "copy edges");
-        UP_CK(cudaMallocAsync(&d_elabels, (size_t)g.nel * 4, s), "alloc edge labels");
-        UP_CK(cudaMemcpyAsync(d_elabels, g.elabel_of_rank.data(), (size_t)g.nel * 4, cudaMemcpyHostToDevice, s),
-              "copy edge labels");
         UP_CK(cudaMallocAsync(&d_tmp, (size_t)m * 8, s), "alloc keys");
         UP_CK(cudaMallocAsync(&g.adj, (size_t)m * 8, s), "alloc adjacency");
         UP_CK(cudaMallocAsync(&g.src, (size_t)m * 4, s), "alloc sources");
     }
     UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
-    UP_CK(gs::launch_build_adjacency(g.offsets, d_edges, g.vrank, d_elabels, g.nel, g, d_tmp, ctx->d_status, s),
+    UP_CK(gs::launch_build_adjacency(g.offsets, d_edges, d_etab, elo, d_elabels, g, d_tmp, ctx->d_status, s),
           "build adjacency launch");
     // Per-vertex masks of the (edge label, to label) segments present, for the
     // mask extension path; only when the tuple space fits the mask width.
@@ -265,36 +330,25 @@ gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t n, int32_t m, const int3
     uint32_t status = 0;
     UP_CK(cudaMemcpyAsync(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
     cleanup();
-    d_edges = nullptr;
-    d_elabels = nullptr;
-    d_tmp = nullptr;
     UP_CK(cudaStreamSynchronize(s), "graph upload");
-#undef UP_CK
     if (status & gs::kErrBadGraph) {
-        free_graph(gr, s);
-        cudaStreamSynchronize(s);
-        delete gr;
+        drop();
         return fail(ctx, GSPAN_ERR_INVALID, "malformed graph: offsets not monotone, an entry's `from` differs from "
                                             "its vertex, or a `to` is out of range");
     }
     // Self-loop bits and the symmetry check, on the validated adjacency.
     {
         const size_t words = ((size_t)n + 31) / 32 + 1;
-        cudaError_t e2;
         uint32_t flags = 0;
-        if ((e2 = cudaMallocAsync(&g.selfloop, words * 4, s)) != cudaSuccess ||
-            (e2 = cudaMemsetAsync(g.selfloop, 0, words * 4, s)) != cudaSuccess ||
-            (e2 = cudaMemsetAsync(ctx->d_status, 0, 4, s)) != cudaSuccess ||
-            (e2 = gs::launch_graph_flags(g, ctx->d_status, s)) != cudaSuccess ||
-            (e2 = cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-            (e2 = cudaStreamSynchronize(s)) != cudaSuccess) {
-            free_graph(gr, s);
-            cudaStreamSynchronize(s);
-            delete gr;
-            return cuda_fail(ctx, e2, "graph flags");
-        }
+        UP_CK(cudaMallocAsync(&g.selfloop, words * 4, s), "alloc self-loop bits");
+        UP_CK(cudaMemsetAsync(g.selfloop, 0, words * 4, s), "clear self-loop bits");
+        UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
+        UP_CK(gs::launch_graph_flags(g, ctx->d_status, s), "graph flags launch");
+        UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
+        UP_CK(cudaStreamSynchronize(s), "graph flags");
         g.symmetric = !(flags & gs::kErrAsymmetric);
     }
+#undef UP_CK
     ++ctx->live_graphs;
     *out = gr;
     return GSPAN_OK;

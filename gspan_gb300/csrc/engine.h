@@ -153,10 +153,20 @@ struct ExpandArgs {
 };
 
 // Kernel launchers (kernels.cu).  All are asynchronous on `st`.
-cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d_edges,
-                                   const int32_t* d_vrank_of_vertex, const int32_t* d_elabels_sorted,
-                                   int32_t nel, DevGraph& g, uint64_t* d_tmp, uint32_t* d_status,
-                                   cudaStream_t st);
+// Graph store build: label min/max ([vmin, vmax, emin, emax], initialised
+// by the caller to INT32_MAX / INT32_MIN), presence flags over the label
+// ranges, vertex label ranks from a dense table, then packed + sorted entries.
+cudaError_t launch_label_minmax(int32_t n, const int32_t* d_vlabels, int32_t m, const gspan_edge* d_edges,
+                                int32_t* d_out, cudaStream_t st);
+cudaError_t launch_label_presence(int32_t n, const int32_t* d_vlabels, int32_t vlo, uint8_t* d_vflag, int32_t m,
+                                  const gspan_edge* d_edges, int32_t elo, uint8_t* d_eflag, cudaStream_t st);
+cudaError_t launch_vertex_ranks(int32_t n, const int32_t* d_vlabels, int32_t vlo, const int32_t* d_vtab,
+                                int32_t* d_vrank, cudaStream_t st);
+// Edge-label ranks from d_etab[label - elo] when d_etab is set, else by binary
+// search over d_elabels_sorted (g.nel entries).  g.vrank must be filled.
+cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d_edges, const int32_t* d_etab,
+                                   int32_t elo, const int32_t* d_elabels_sorted, DevGraph& g, uint64_t* d_tmp,
+                                   uint32_t* d_status, cudaStream_t st);
 cudaError_t launch_seed_count(const DevGraph& g, unsigned long long* counts, cudaStream_t st);
 cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* pool, int32_t* col0,
                                 int32_t* col1, uint32_t* status, cudaStream_t st);

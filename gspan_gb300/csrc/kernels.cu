@@ -94,9 +94,60 @@ __device__ __forceinline__ int32_t lower_bound_entry(const uint64_t* __restrict_
 // ---------------------------------------------------------------------------
 // Graph store build.
 
+// Label ranks on the device: min/max, then presence flags over the value
+// range; the host turns the flags into rank tables.
+__global__ void k_label_minmax(int32_t n, const int32_t* __restrict__ vlabels, int32_t m,
+                               const gspan_edge* __restrict__ edges, int32_t* __restrict__ out)
+{
+    int32_t vmin = INT32_MAX, vmax = INT32_MIN, emin = INT32_MAX, emax = INT32_MIN;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        vmin = min(vmin, vlabels[i]);
+        vmax = max(vmax, vlabels[i]);
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
+        emin = min(emin, edges[i].label);
+        emax = max(emax, edges[i].label);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        vmin = min(vmin, __shfl_xor_sync(kFull, vmin, o));
+        vmax = max(vmax, __shfl_xor_sync(kFull, vmax, o));
+        emin = min(emin, __shfl_xor_sync(kFull, emin, o));
+        emax = max(emax, __shfl_xor_sync(kFull, emax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(out + 0, vmin);
+        atomicMax(out + 1, vmax);
+        atomicMin(out + 2, emin);
+        atomicMax(out + 3, emax);
+    }
+}
+
+__global__ void k_label_presence(int32_t n, const int32_t* __restrict__ vlabels, int32_t vlo,
+                                 uint8_t* __restrict__ vflag, int32_t m, const gspan_edge* __restrict__ edges,
+                                 int32_t elo, uint8_t* __restrict__ eflag)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+        vflag[(int64_t)vlabels[i] - vlo] = 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride)
+        eflag[(int64_t)edges[i].label - elo] = 1;
+}
+
+__global__ void k_vertex_ranks(int32_t n, const int32_t* __restrict__ vlabels, int32_t vlo,
+                               const int32_t* __restrict__ vtab, int32_t* __restrict__ vrank)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        vrank[i] = vtab[(int64_t)vlabels[i] - vlo];
+}
+
+// Packed key of every entry.  Edge-label ranks come from a dense table
+// (etab, indexed by label - elo) or, for sparse label ranges, from a binary
+// search over the sorted distinct labels.
 __global__ void k_entry_keys(int32_t m, int32_t n, const gspan_edge* __restrict__ edges,
-                             const int32_t* __restrict__ vrank, const int32_t* __restrict__ elabels,
-                             int32_t nel, uint64_t* __restrict__ keys, uint32_t* status)
+                             const int32_t* __restrict__ vrank, const int32_t* __restrict__ etab, int32_t elo,
+                             const int32_t* __restrict__ elabels, int32_t nel, uint64_t* __restrict__ keys,
+                             uint32_t* status)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const gspan_edge e = edges[i];
@@ -105,22 +156,36 @@ __global__ void k_entry_keys(int32_t m, int32_t n, const gspan_edge* __restrict_
             keys[i] = 0;
             continue;
         }
-        int32_t lo = 0, hi = nel - 1;
-        while (lo < hi) {
-            const int32_t mid = (lo + hi) >> 1;
-            if (elabels[mid] < e.label) lo = mid + 1; else hi = mid;
+        int32_t lo;
+        if (etab) {
+            lo = etab[(int64_t)e.label - elo];
+        } else {
+            lo = 0;
+            int32_t hi = nel - 1;
+            while (lo < hi) {
+                const int32_t mid = (lo + hi) >> 1;
+                if (elabels[mid] < e.label) lo = mid + 1; else hi = mid;
+            }
         }
         keys[i] = pack_entry((uint32_t)lo, (uint32_t)vrank[e.to], (uint32_t)e.to);
     }
 }
 
-// Warp per vertex: every entry's final slot is its rank inside the segment
-// (ties broken by original position), so the sort is stable and needs no
-// scratch beyond the unsorted keys.
-__global__ void k_sort_segments(int32_t n, int32_t m, const int32_t* __restrict__ offsets,
-                                const gspan_edge* __restrict__ edges, const uint64_t* __restrict__ keys,
-                                uint64_t* __restrict__ adj, int32_t* __restrict__ src, uint32_t* status)
+constexpr int kSortBuckets = 128;
+
+// Warp per vertex.  The reference's CSR lists each adjacency by (to, label);
+// then a stable counting sort by the (edge label, to label) tuple yields the
+// (edge label, to label, to) order in O(degree).  Input in any other order,
+// or a tuple space wider than kSortBuckets, falls back to ranking every entry
+// against its segment (O(degree^2), still stable).
+__global__ void __launch_bounds__(256) k_sort_segments(int32_t n, int32_t m, int32_t nvl, int32_t K,
+                                                       const int32_t* __restrict__ offsets,
+                                                       const gspan_edge* __restrict__ edges,
+                                                       const uint64_t* __restrict__ keys, uint64_t* __restrict__ adj,
+                                                       int32_t* __restrict__ src, uint32_t* status)
 {
+    __shared__ uint32_t cnt_s[8][kSortBuckets];
+    uint32_t* cnt = cnt_s[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -130,16 +195,75 @@ __global__ void k_sort_segments(int32_t n, int32_t m, const int32_t* __restrict_
             if (lane == 0) atomicOr(status, kErrBadGraph);
             continue;
         }
+        bool sorted = true;
         for (int32_t j = b + lane; j < e; j += 32) {
-            if (edges[j].from != (int32_t)v) atomicOr(status, kErrBadGraph);
-            const uint64_t kj = __ldg(keys + j);
-            int32_t rank = 0;
-            for (int32_t i = b; i < e; ++i) {
-                const uint64_t ki = __ldg(keys + i);
-                rank += (ki < kj) || (ki == kj && i < j);
-            }
-            adj[b + rank] = kj;
+            const gspan_edge c = edges[j];
+            if (c.from != (int32_t)v) atomicOr(status, kErrBadGraph);
             src[j] = (int32_t)v;
+            if (j > b) {
+                const gspan_edge pv = edges[j - 1];
+                sorted &= pv.to < c.to || (pv.to == c.to && pv.label <= c.label);
+            }
+        }
+        sorted = __all_sync(kFull, sorted);
+        if (!sorted || K > kSortBuckets) {
+            for (int32_t j = b + lane; j < e; j += 32) {
+                const uint64_t kj = __ldg(keys + j);
+                int32_t rank = 0;
+                for (int32_t i = b; i < e; ++i) {
+                    const uint64_t ki = __ldg(keys + i);
+                    rank += (ki < kj) || (ki == kj && i < j);
+                }
+                adj[b + rank] = kj;
+            }
+            continue;
+        }
+        for (int i = lane; i < kSortBuckets; i += 32) cnt[i] = 0;
+        __syncwarp();
+        for (int32_t j = b + lane; j < e; j += 32) {
+            const uint64_t kj = __ldg(keys + j);
+            atomicAdd(&cnt[entry_el(kj) * (uint32_t)nvl + entry_tl(kj)], 1u);
+        }
+        __syncwarp();
+        // Exclusive scan of the bucket counts; lane i owns buckets 4i .. 4i+3.
+        uint32_t c[4], local = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            c[q] = cnt[4 * lane + q];
+            local += c[q];
+        }
+        uint32_t incl = local;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, incl, d);
+            if (lane >= d) incl += t;
+        }
+        uint32_t run = incl - local;
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            cnt[4 * lane + q] = run;
+            run += c[q];
+        }
+        __syncwarp();
+        for (int32_t base = b; base < e; base += 32) {
+            const int32_t j = base + lane;
+            const bool valid = j < e;
+            uint64_t kj = 0;
+            uint32_t bucket = 0;
+            if (valid) {
+                kj = __ldg(keys + j);
+                bucket = entry_el(kj) * (uint32_t)nvl + entry_tl(kj);
+            }
+            const unsigned vm = __ballot_sync(kFull, valid);
+            unsigned peers = 0;
+            if (valid) {
+                peers = __match_any_sync(vm, bucket);
+                adj[b + cnt[bucket] + __popc(peers & lanemask_lt())] = kj;
+            }
+            __syncwarp();
+            if (valid && lane == __ffs(peers) - 1) cnt[bucket] += __popc(peers);
+            __syncwarp();
         }
     }
 }
@@ -871,18 +995,40 @@ int grid_for(int64_t work, int threads)
 
 }  // namespace
 
-cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d_edges,
-                                   const int32_t* d_vrank_of_vertex, const int32_t* d_elabels_sorted,
-                                   int32_t nel, DevGraph& g, uint64_t* d_tmp, uint32_t* d_status,
-                                   cudaStream_t st)
+cudaError_t launch_label_minmax(int32_t n, const int32_t* d_vlabels, int32_t m, const gspan_edge* d_edges,
+                                int32_t* d_out, cudaStream_t st)
+{
+    k_label_minmax<<<grid_for(std::max<int64_t>(n, m), 256), 256, 0, st>>>(n, d_vlabels, m, d_edges, d_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_label_presence(int32_t n, const int32_t* d_vlabels, int32_t vlo, uint8_t* d_vflag, int32_t m,
+                                  const gspan_edge* d_edges, int32_t elo, uint8_t* d_eflag, cudaStream_t st)
+{
+    k_label_presence<<<grid_for(std::max<int64_t>(n, m), 256), 256, 0, st>>>(n, d_vlabels, vlo, d_vflag, m, d_edges,
+                                                                             elo, d_eflag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vertex_ranks(int32_t n, const int32_t* d_vlabels, int32_t vlo, const int32_t* d_vtab,
+                                int32_t* d_vrank, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    k_vertex_ranks<<<grid_for(n, 256), 256, 0, st>>>(n, d_vlabels, vlo, d_vtab, d_vrank);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d_edges, const int32_t* d_etab,
+                                   int32_t elo, const int32_t* d_elabels_sorted, DevGraph& g, uint64_t* d_tmp,
+                                   uint32_t* d_status, cudaStream_t st)
 {
     if (g.m > 0) {
-        k_entry_keys<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.n, d_edges, d_vrank_of_vertex, d_elabels_sorted,
-                                                         nel, d_tmp, d_status);
+        k_entry_keys<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.n, d_edges, g.vrank, d_etab, elo, d_elabels_sorted,
+                                                         g.nel, d_tmp, d_status);
     }
     if (g.n > 0) {
-        k_sort_segments<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, d_offsets, d_edges, d_tmp,
-                                                                          g.adj, g.src, d_status);
+        k_sort_segments<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, g.nvl, g.nel * g.nvl, d_offsets,
+                                                                          d_edges, d_tmp, g.adj, g.src, d_status);
     }
     return cudaGetLastError();
 }

@@ -112,3 +112,34 @@ def test_fsm_cli_matches_golden():
                              capture_output=True, text=True, check=True).stdout.splitlines()
     assert out[-1].startswith("load:")
     assert out[:-1] == golden_lines(case)
+
+
+def test_unsorted_adjacency_input(miner):
+    """Adjacency lists not in (to, label) order take the rank-sort fallback of
+    the upload; with one edge label the reference's output does not depend on
+    that order."""
+    import numpy as np
+    from gspan_gb300 import datagen
+    case = [c for c in golden_cases() if c["name"] == "er3300" and c["min_support"] == 50][0]
+    g = golden_graph(case)
+    rng = np.random.default_rng(3)
+    edges = g.edges.copy()
+    for v in range(g.n):
+        b, e = g.offsets[v], g.offsets[v + 1]
+        edges[b:e] = edges[b:e][rng.permutation(e - b)]
+    shuffled = datagen.CSR(g.offsets, g.vlabels, edges)
+    patterns, _ = miner.fsm(shuffled, case["k"], case["min_support"])
+    assert lines_of(patterns) == golden_lines(case)
+
+
+def test_wide_label_space(miner):
+    """150 vertex labels: the tuple space exceeds the mask width, so the upload
+    ranks entries without the counting sort and only the per-candidate kernels
+    run; the output still equals the oracle's."""
+    from gspan_gb300 import datagen
+    g = datagen.erdos_renyi(3000, 9000, 150, 41, nelabels=2)
+    want, st = run_port(g, 3, 3, threads=4, with_stats=True)
+    patterns, got = miner.fsm(g, 3, 3)
+    assert lines_of(patterns) == want
+    assert got["extended"] == st["extended"]
+    assert got["mask_parents"] == 0
