@@ -63,6 +63,7 @@ class Stats(ctypes.Structure):
                 ("scanned_entries", ctypes.c_uint64), ("materialized_rows", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint64), ("levels", ctypes.c_int32), ("mine_ms", ctypes.c_double),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("frontier_rows", ctypes.c_uint64),
                 ("mask_parents", ctypes.c_uint64), ("candidate_parents", ctypes.c_uint64),
                 ("expand_ms", ctypes.c_double), ("expand_launches", ctypes.c_uint64),
                 ("expand_bytes", ctypes.c_double),
@@ -99,6 +100,17 @@ _lib.gspan_graph_free.restype = ctypes.c_int
 _lib.gspan_mine.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, EMIT_FN,
                             ctypes.c_void_p, ctypes.POINTER(Stats)]
 _lib.gspan_mine.restype = ctypes.c_int
+BATCH_EMIT_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(PatternEdge),
+                                 ctypes.c_int32, ctypes.c_int32)
+_lib.gspan_batch_upload.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.POINTER(ctypes.c_void_p)]
+_lib.gspan_batch_upload.restype = ctypes.c_int
+_lib.gspan_mine_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                  BATCH_EMIT_FN, ctypes.c_void_p, ctypes.POINTER(Stats)]
+_lib.gspan_mine_batch.restype = ctypes.c_int
+_lib.gspan_graph_instances.argtypes = [ctypes.c_void_p]
+_lib.gspan_graph_instances.restype = ctypes.c_int32
 _lib.gspan_table_support.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]
 _lib.gspan_table_support.restype = ctypes.c_int
@@ -116,7 +128,8 @@ _lib.gspan_max_pattern_edges.restype = ctypes.c_int32
 
 # Every symbol include/gspan_gb300.h declares (checked by the tests).
 ABI_SYMBOLS = ("gspan_opts_default", "gspan_ctx_create", "gspan_ctx_destroy", "gspan_graph_upload",
-               "gspan_graph_free", "gspan_mine", "gspan_table_support", "gspan_table_support_noalloc",
+               "gspan_graph_free", "gspan_mine", "gspan_batch_upload", "gspan_mine_batch", "gspan_graph_instances",
+               "gspan_table_support", "gspan_table_support_noalloc",
                "gspan_is_canonical",
                "gspan_status_string", "gspan_last_error", "gspan_max_pattern_edges")
 
@@ -216,6 +229,44 @@ class Miner:
         rc = _lib.gspan_mine(self._ctx, dg.handle, int(k), int(min_support), cb, None, ctypes.byref(st))
         if rc != GSPAN_OK:
             raise self._err(rc, "gspan_mine")
+        return out, st.as_dict()
+
+    def upload_batch(self, graphs) -> DeviceGraph:
+        """Uploads many independent graphs as one batch (gspan_batch_upload)."""
+        arrs = [(np.ascontiguousarray(g.offsets, dtype=np.int32), np.ascontiguousarray(g.vlabels, dtype=np.int32),
+                 np.ascontiguousarray(g.edges, dtype=np.int32).reshape(-1, 3)) for g in graphs]
+        k = len(arrs)
+        ns = np.array([a[1].shape[0] for a in arrs], dtype=np.int32)
+        ms = np.array([a[2].shape[0] for a in arrs], dtype=np.int32)
+        offs = (ctypes.c_void_p * k)(*[a[0].ctypes.data for a in arrs])
+        vls = (ctypes.c_void_p * k)(*[a[1].ctypes.data if a[1].size else None for a in arrs])
+        eds = (ctypes.c_void_p * k)(*[a[2].ctypes.data if a[2].size else None for a in arrs])
+        h = ctypes.c_void_p()
+        rc = _lib.gspan_batch_upload(self._ctx, k, ns.ctypes.data, ms.ctypes.data, offs, vls, eds, ctypes.byref(h))
+        if rc != GSPAN_OK:
+            raise self._err(rc, "gspan_batch_upload")
+        dg = DeviceGraph(h, int(ns.sum()), int(ms.sum()))
+        self._graphs.append(dg)
+        return dg
+
+    def mine_batch(self, dg: DeviceGraph, k: int, min_supports):
+        """Returns (per-instance pattern lists, stats); each list as mine()."""
+        ninst = int(_lib.gspan_graph_instances(dg.handle))
+        out: list = [[] for _ in range(ninst)]
+
+        def emit(_user, inst, code, length, support):
+            out[inst].append((tuple((code[i].frm, code[i].to, code[i].from_label, code[i].edge_label,
+                                     code[i].to_label) for i in range(length)), int(support)))
+            return 0
+
+        cb = BATCH_EMIT_FN(emit)
+        sups = np.ascontiguousarray(min_supports, dtype=np.int32)
+        if sups.shape[0] != ninst:
+            raise ValueError("one min_support per instance")
+        st = Stats()
+        rc = _lib.gspan_mine_batch(self._ctx, dg.handle, int(k), sups.ctypes.data, cb, None, ctypes.byref(st))
+        if rc != GSPAN_OK:
+            raise self._err(rc, "gspan_mine_batch")
         return out, st.as_dict()
 
     def table_support(self, cols, nr_nodes: int):

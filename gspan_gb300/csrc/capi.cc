@@ -19,67 +19,6 @@ using gs::fail;
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
     } while (0)
 
-// Ranks of the distinct values of `vals` (ascending).  Small value ranges use
-// a presence table, anything else a sort.
-void rank_labels(const int32_t* vals, size_t n, size_t stride_ints, std::vector<int32_t>& distinct,
-                 std::vector<int32_t>* rank_of_each)
-{
-    distinct.clear();
-    if (n == 0) {
-        if (rank_of_each) rank_of_each->clear();
-        return;
-    }
-    int64_t lo = vals[0], hi = vals[0];
-    for (size_t i = 0; i < n; ++i) {
-        const int64_t v = vals[i * stride_ints];
-        lo = std::min(lo, v);
-        hi = std::max(hi, v);
-    }
-    const int64_t range = hi - lo + 1;
-    if (range <= (int64_t)1 << 22) {
-        std::vector<int32_t> slot((size_t)range, -1);
-        for (size_t i = 0; i < n; ++i) slot[(size_t)(vals[i * stride_ints] - lo)] = 0;
-        int32_t r = 0;
-        for (int64_t v = 0; v < range; ++v)
-            if (slot[(size_t)v] == 0) {
-                slot[(size_t)v] = r++;
-                distinct.push_back((int32_t)(v + lo));
-            }
-        if (rank_of_each) {
-            rank_of_each->resize(n);
-            for (size_t i = 0; i < n; ++i) (*rank_of_each)[i] = slot[(size_t)(vals[i * stride_ints] - lo)];
-        }
-        return;
-    }
-    distinct.reserve(n);
-    for (size_t i = 0; i < n; ++i) distinct.push_back(vals[i * stride_ints]);
-    std::sort(distinct.begin(), distinct.end());
-    distinct.erase(std::unique(distinct.begin(), distinct.end()), distinct.end());
-    if (rank_of_each) {
-        rank_of_each->resize(n);
-        for (size_t i = 0; i < n; ++i)
-            (*rank_of_each)[i] =
-                (int32_t)(std::lower_bound(distinct.begin(), distinct.end(), vals[i * stride_ints]) - distinct.begin());
-    }
-}
-
-void free_graph(gspan_graph* gr, cudaStream_t st)
-{
-    gs::DevGraph& g = gr->g;
-    if (g.offsets) cudaFreeAsync(g.offsets, st);
-    if (g.adj) cudaFreeAsync(g.adj, st);
-    if (g.src) cudaFreeAsync(g.src, st);
-    if (g.vrank) cudaFreeAsync(g.vrank, st);
-    if (g.segmask) cudaFreeAsync(g.segmask, st);
-    if (g.selfloop) cudaFreeAsync(g.selfloop, st);
-    g.segmask = nullptr;
-    g.selfloop = nullptr;
-    g.offsets = nullptr;
-    g.adj = nullptr;
-    g.src = nullptr;
-    g.vrank = nullptr;
-}
-
 }  // namespace
 
 extern "C" {
@@ -180,178 +119,21 @@ gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t n, int32_t m, const int3
 {
     if (!ctx || !out) return GSPAN_ERR_INVALID;
     *out = nullptr;
-    if (n < 0 || m < 0) return fail(ctx, GSPAN_ERR_INVALID, "negative graph size");
-    if (!offsets || (n > 0 && !vlabels) || (m > 0 && !edges))
-        return fail(ctx, GSPAN_ERR_INVALID, "null graph array");
-    if (offsets[0] != 0 || offsets[n] != m)
-        return fail(ctx, GSPAN_ERR_INVALID, "offsets must start at 0 and end at nr_edges");
-    GS_CK(cudaSetDevice(ctx->device), "set device");
-    cudaStream_t s = ctx->stream;
+    const int32_t ns[1] = {n}, ms[1] = {m};
+    const int32_t* offs[1] = {offsets};
+    const int32_t* vls[1] = {vlabels};
+    const gspan_edge* eds[1] = {edges};
+    return gs::upload_graphs(ctx, 1, ns, ms, offs, vls, eds, out);
+}
 
-    gspan_graph* gr = new (std::nothrow) gspan_graph();
-    if (!gr) return fail(ctx, GSPAN_ERR_NOMEM, "host allocation");
-    gr->owner = ctx;
-    gs::DevGraph& g = gr->g;
-    g.n = n;
-    g.m = m;
-
-    // Temporaries of the build, freed on every path.
-    gspan_edge* d_edges = nullptr;
-    int32_t *d_vl = nullptr, *d_minmax = nullptr, *d_vtab = nullptr, *d_etab = nullptr, *d_elabels = nullptr;
-    uint8_t *d_vflag = nullptr, *d_eflag = nullptr;
-    uint64_t* d_tmp = nullptr;
-    auto cleanup = [&]() {
-        for (void* p : {(void*)d_edges, (void*)d_vl, (void*)d_minmax, (void*)d_vtab, (void*)d_etab, (void*)d_elabels,
-                        (void*)d_vflag, (void*)d_eflag, (void*)d_tmp})
-            if (p) cudaFreeAsync(p, s);
-        d_edges = nullptr;
-        d_vl = d_minmax = d_vtab = d_etab = d_elabels = nullptr;
-        d_vflag = d_eflag = nullptr;
-        d_tmp = nullptr;
-    };
-    auto drop = [&]() {
-        cleanup();
-        free_graph(gr, s);
-        cudaStreamSynchronize(s);
-        delete gr;
-    };
-    auto bail = [&](cudaError_t e, const char* what) {
-        drop();
-        return cuda_fail(ctx, e, what);
-    };
-    cudaError_t e;
-#define UP_CK(call, what) \
-    if ((e = (call)) != cudaSuccess) return bail(e, what)
-    UP_CK(cudaMallocAsync(&g.offsets, ((size_t)n + 1) * 4, s), "alloc offsets");
-    UP_CK(cudaMemcpyAsync(g.offsets, offsets, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice, s), "copy offsets");
-    if (n > 0) {
-        UP_CK(cudaMallocAsync(&d_vl, (size_t)n * 4, s), "alloc labels");
-        UP_CK(cudaMemcpyAsync(d_vl, vlabels, (size_t)n * 4, cudaMemcpyHostToDevice, s), "copy labels");
-        UP_CK(cudaMallocAsync(&g.vrank, (size_t)n * 4, s), "alloc vrank");
-    }
-    if (m > 0) {
-        UP_CK(cudaMallocAsync(&d_edges, (size_t)m * sizeof(gspan_edge), s), "alloc edges");
-        UP_CK(cudaMemcpyAsync(d_edges, edges, (size_t)m * sizeof(gspan_edge), cudaMemcpyHostToDevice, s),
-              "copy edges");
-    }
-
-    // Label ranks: min/max and presence on the device, rank tables on the host
-    // (O(label range)); sparse ranges beyond 2^24 values rank on the host.
-    constexpr int64_t kDenseRange = (int64_t)1 << 24;
-    int32_t mm[4] = {INT32_MAX, INT32_MIN, INT32_MAX, INT32_MIN};
-    UP_CK(cudaMallocAsync(&d_minmax, sizeof(mm), s), "alloc minmax");
-    UP_CK(cudaMemcpyAsync(d_minmax, mm, sizeof(mm), cudaMemcpyHostToDevice, s), "init minmax");
-    if (n > 0 || m > 0) UP_CK(gs::launch_label_minmax(n, d_vl, m, d_edges, d_minmax, s), "label minmax launch");
-    UP_CK(cudaMemcpyAsync(mm, d_minmax, sizeof(mm), cudaMemcpyDeviceToHost, s), "read minmax");
-    UP_CK(cudaStreamSynchronize(s), "label minmax");
-    const int64_t vrange = n > 0 ? (int64_t)mm[1] - mm[0] + 1 : 0;
-    const int64_t erange = m > 0 ? (int64_t)mm[3] - mm[2] + 1 : 0;
-    int32_t elo = mm[2];
-    if (vrange <= kDenseRange && erange <= kDenseRange) {
-        std::vector<uint8_t> vflag((size_t)vrange), eflag((size_t)erange);
-        if (vrange) UP_CK(cudaMallocAsync(&d_vflag, (size_t)vrange, s), "alloc flags");
-        if (erange) UP_CK(cudaMallocAsync(&d_eflag, (size_t)erange, s), "alloc flags");
-        if (vrange) UP_CK(cudaMemsetAsync(d_vflag, 0, (size_t)vrange, s), "clear flags");
-        if (erange) UP_CK(cudaMemsetAsync(d_eflag, 0, (size_t)erange, s), "clear flags");
-        UP_CK(gs::launch_label_presence(n, d_vl, mm[0], d_vflag, m, d_edges, elo, d_eflag, s), "presence launch");
-        if (vrange) UP_CK(cudaMemcpyAsync(vflag.data(), d_vflag, (size_t)vrange, cudaMemcpyDeviceToHost, s), "flags");
-        if (erange) UP_CK(cudaMemcpyAsync(eflag.data(), d_eflag, (size_t)erange, cudaMemcpyDeviceToHost, s), "flags");
-        UP_CK(cudaStreamSynchronize(s), "label presence");
-        std::vector<int32_t> vtab((size_t)vrange, -1), etab((size_t)erange, -1);
-        for (int64_t v = 0; v < vrange; ++v)
-            if (vflag[(size_t)v]) {
-                vtab[(size_t)v] = (int32_t)g.vlabel_of_rank.size();
-                g.vlabel_of_rank.push_back((int32_t)(v + mm[0]));
-            }
-        for (int64_t v = 0; v < erange; ++v)
-            if (eflag[(size_t)v]) {
-                etab[(size_t)v] = (int32_t)g.elabel_of_rank.size();
-                g.elabel_of_rank.push_back((int32_t)(v + elo));
-            }
-        if (vrange) {
-            UP_CK(cudaMallocAsync(&d_vtab, (size_t)vrange * 4, s), "alloc rank table");
-            UP_CK(cudaMemcpyAsync(d_vtab, vtab.data(), (size_t)vrange * 4, cudaMemcpyHostToDevice, s), "rank table");
-            UP_CK(gs::launch_vertex_ranks(n, d_vl, mm[0], d_vtab, g.vrank, s), "vertex ranks launch");
-        }
-        if (erange) {
-            UP_CK(cudaMallocAsync(&d_etab, (size_t)erange * 4, s), "alloc rank table");
-            UP_CK(cudaMemcpyAsync(d_etab, etab.data(), (size_t)erange * 4, cudaMemcpyHostToDevice, s), "rank table");
-        }
-        UP_CK(cudaStreamSynchronize(s), "rank tables");   // host tables leave scope
-    } else {
-        std::vector<int32_t> vrank;
-        rank_labels(vlabels, (size_t)n, 1, g.vlabel_of_rank, &vrank);
-        rank_labels(m > 0 ? &edges[0].label : nullptr, (size_t)m, 3, g.elabel_of_rank, nullptr);
-        if (n > 0)
-            UP_CK(cudaMemcpyAsync(g.vrank, vrank.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s), "copy vrank");
-        if (!g.elabel_of_rank.empty()) {
-            UP_CK(cudaMallocAsync(&d_elabels, g.elabel_of_rank.size() * 4, s), "alloc edge labels");
-            UP_CK(cudaMemcpyAsync(d_elabels, g.elabel_of_rank.data(), g.elabel_of_rank.size() * 4,
-                                  cudaMemcpyHostToDevice, s),
-                  "copy edge labels");
-        }
-        UP_CK(cudaStreamSynchronize(s), "host ranks");
-    }
-    g.nvl = (int32_t)g.vlabel_of_rank.size();
-    g.nel = (int32_t)g.elabel_of_rank.size();
-    if (g.nvl > 0xFFFF || g.nel > 0xFFFF) {
-        drop();
-        return fail(ctx, GSPAN_ERR_LIMIT, "more than 65535 distinct vertex or edge labels");
-    }
-    // Mean degree behind an edge, for the kernel-path choice.
-    {
-        double d1 = 0, d2 = 0;
-        for (int32_t v = 0; v < n; ++v) {
-            const double d = (double)offsets[v + 1] - offsets[v];
-            d1 += d;
-            d2 += d * d;
-        }
-        g.edge_biased_degree = d1 > 0 ? d2 / d1 : 0.0;
-    }
-
-    if (m > 0) {
-        UP_CK(cudaMallocAsync(&d_tmp, (size_t)m * 8, s), "alloc keys");
-        UP_CK(cudaMallocAsync(&g.adj, (size_t)m * 8, s), "alloc adjacency");
-        UP_CK(cudaMallocAsync(&g.src, (size_t)m * 4, s), "alloc sources");
-    }
-    UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
-    UP_CK(gs::launch_build_adjacency(g.offsets, d_edges, d_etab, elo, d_elabels, g, d_tmp, ctx->d_status, s),
-          "build adjacency launch");
-    // Per-vertex masks of the (edge label, to label) segments present, for the
-    // mask extension path; only when the tuple space fits the mask width.
-    {
-        const int64_t K = (int64_t)g.nel * g.nvl;
-        if (n > 0 && K > 0 && K <= 32 * gs::kMaxMaskWords) {
-            g.segw = (int32_t)((K + 31) / 32);
-            UP_CK(cudaMallocAsync(&g.segmask, (size_t)n * g.segw * 4, s), "alloc segment masks");
-            UP_CK(gs::launch_segmask(g, s), "segment mask launch");
-        }
-    }
-    uint32_t status = 0;
-    UP_CK(cudaMemcpyAsync(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
-    cleanup();
-    UP_CK(cudaStreamSynchronize(s), "graph upload");
-    if (status & gs::kErrBadGraph) {
-        drop();
-        return fail(ctx, GSPAN_ERR_INVALID, "malformed graph: offsets not monotone, an entry's `from` differs from "
-                                            "its vertex, or a `to` is out of range");
-    }
-    // Self-loop bits and the symmetry check, on the validated adjacency.
-    {
-        const size_t words = ((size_t)n + 31) / 32 + 1;
-        uint32_t flags = 0;
-        UP_CK(cudaMallocAsync(&g.selfloop, words * 4, s), "alloc self-loop bits");
-        UP_CK(cudaMemsetAsync(g.selfloop, 0, words * 4, s), "clear self-loop bits");
-        UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
-        UP_CK(gs::launch_graph_flags(g, ctx->d_status, s), "graph flags launch");
-        UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
-        UP_CK(cudaStreamSynchronize(s), "graph flags");
-        g.symmetric = !(flags & gs::kErrAsymmetric);
-    }
-#undef UP_CK
-    ++ctx->live_graphs;
-    *out = gr;
-    return GSPAN_OK;
+gspan_status gspan_batch_upload(gspan_ctx* ctx, int32_t ninst, const int32_t* nr_nodes, const int32_t* nr_edges,
+                                const int32_t* const* offsets, const int32_t* const* vlabels,
+                                const gspan_edge* const* edges, gspan_graph** out)
+{
+    if (!ctx || !out || ninst < 1 || !nr_nodes || !nr_edges || !offsets || !vlabels || !edges)
+        return GSPAN_ERR_INVALID;
+    *out = nullptr;
+    return gs::upload_graphs(ctx, ninst, nr_nodes, nr_edges, offsets, vlabels, edges, out);
 }
 
 gspan_status gspan_graph_free(gspan_ctx* ctx, gspan_graph* graph)
@@ -359,7 +141,7 @@ gspan_status gspan_graph_free(gspan_ctx* ctx, gspan_graph* graph)
     if (!ctx || !graph) return GSPAN_ERR_INVALID;
     if (graph->owner != ctx) return fail(ctx, GSPAN_ERR_INVALID, "graph belongs to another context");
     cudaSetDevice(ctx->device);
-    free_graph(graph, ctx->stream);
+    gs::free_graph(graph, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     delete graph;
     --ctx->live_graphs;
@@ -372,15 +154,50 @@ gspan_status gspan_mine(gspan_ctx* ctx, const gspan_graph* graph, int32_t k, int
     if (!ctx || !graph) return GSPAN_ERR_INVALID;
     if (graph->owner != ctx) return fail(ctx, GSPAN_ERR_INVALID, "graph belongs to another context");
     ctx->err.clear();
+    if (graph->g.ninst != 1) return fail(ctx, GSPAN_ERR_INVALID, "a batch is mined with gspan_mine_batch");
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "set device");
     try {
-        return gs::mine(ctx, graph->g, k, min_support, emit, user, stats);
+        const std::vector<int32_t> minsup{min_support};
+        gs::EmitFn fn;
+        if (emit)
+            fn = [emit, user](int, const gspan_pattern_edge* c, int32_t len, int32_t sup) {
+                return emit(user, c, len, sup);
+            };
+        return gs::mine(ctx, graph->g, k, minsup, fn, stats);
     } catch (const std::bad_alloc&) {
         return fail(ctx, GSPAN_ERR_NOMEM, "host allocation failed");
     } catch (const std::exception& ex) {
         return fail(ctx, GSPAN_ERR_INVALID, ex.what());
     }
+}
+
+gspan_status gspan_mine_batch(gspan_ctx* ctx, const gspan_graph* batch, int32_t k, const int32_t* min_support,
+                              gspan_batch_emit_fn emit, void* user, gspan_stats* stats)
+{
+    if (!ctx || !batch || !min_support) return GSPAN_ERR_INVALID;
+    if (batch->owner != ctx) return fail(ctx, GSPAN_ERR_INVALID, "graph belongs to another context");
+    ctx->err.clear();
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "set device");
+    try {
+        const std::vector<int32_t> minsup(min_support, min_support + batch->g.ninst);
+        gs::EmitFn fn;
+        if (emit)
+            fn = [emit, user](int inst, const gspan_pattern_edge* c, int32_t len, int32_t sup) {
+                return emit(user, inst, c, len, sup);
+            };
+        return gs::mine(ctx, batch->g, k, minsup, fn, stats);
+    } catch (const std::bad_alloc&) {
+        return fail(ctx, GSPAN_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& ex) {
+        return fail(ctx, GSPAN_ERR_INVALID, ex.what());
+    }
+}
+
+int32_t gspan_graph_instances(const gspan_graph* graph)
+{
+    return graph ? graph->g.ninst : 0;
 }
 
 gspan_status gspan_is_canonical(const gspan_pattern_edge* code, int32_t len, int32_t* out)

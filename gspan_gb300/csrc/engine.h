@@ -42,6 +42,16 @@ struct DevGraph {
     int32_t n = 0;              // vertices
     int32_t m = 0;              // directed entries (2 per undirected edge)
     int32_t nvl = 0, nel = 0;   // distinct vertex / edge labels
+    int32_t ninst = 1;          // mining instances (independent graphs) in this store
+    // Label windows: the neighbours of a vertex with label rank r have label
+    // ranks in [win_base[r], win_base[r] + lwin).  One window of all labels for
+    // a single graph; one window per instance for a batch (instance-tagged
+    // labels never meet across instances).  Tuple keys are window-local.
+    int32_t lwin = 0;
+    int32_t* win_base = nullptr;        // [nvl] device
+    std::vector<int32_t> win_base_h;    // [nvl] host copy
+    std::vector<int32_t> label_instance;  // [nvl] instance of each label rank (batch)
+    std::vector<int64_t> inst_vbase, inst_ebase;  // [ninst + 1] vertex / entry prefix of the instances
     int32_t* offsets = nullptr; // [n+1]
     uint64_t* adj = nullptr;    // [m] packed entries, sorted per vertex
     int32_t* src = nullptr;     // [m] owning vertex of each entry
@@ -74,6 +84,8 @@ struct DomDesc {
     uint32_t cap;
     uint16_t nvc;
     uint16_t hash;
+    int32_t vbase;              // first vertex of the tuple's instance (ids are stored relative to it)
+    int32_t pad;
 };
 
 constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
@@ -96,6 +108,10 @@ struct ParentMeta {
     int16_t nedge;
     int16_t vn;                 // rightmost vertex v_n
     int16_t min_label;          // vertex-label rank of v0
+    int32_t lbase;              // first label rank of this pattern's label window
+    // Vertices [vbase, vbase + nloc) and entries [ebase, ebase + mloc) of this
+    // pattern's instance: the dense per-parent arrays cover only these.
+    int32_t vbase, nloc, ebase, mloc;
     int16_t vlab[kMaxV];        // vertex-label rank of each pattern vertex
     int16_t src_v[kMaxV];
     int16_t src_el[kMaxV];
@@ -160,6 +176,11 @@ cudaError_t launch_label_minmax(int32_t n, const int32_t* d_vlabels, int32_t m, 
                                 int32_t* d_out, cudaStream_t st);
 cudaError_t launch_label_presence(int32_t n, const int32_t* d_vlabels, int32_t vlo, uint8_t* d_vflag, int32_t m,
                                   const gspan_edge* d_edges, int32_t elo, uint8_t* d_eflag, cudaStream_t st);
+// Batch: instance-local offsets and ids -> batch-wide (vbase/ebase: [ninst+1]
+// prefix sums of vertex and entry counts); an id outside its instance sets
+// kErrBadGraph.
+cudaError_t launch_batch_fixup(int32_t ninst, const int64_t* d_vbase, const int64_t* d_ebase, int32_t N, int32_t M,
+                               int32_t* d_offsets, gspan_edge* d_edges, uint32_t* d_status, cudaStream_t st);
 cudaError_t launch_vertex_ranks(int32_t n, const int32_t* d_vlabels, int32_t vlo, const int32_t* d_vtab,
                                 int32_t* d_vrank, cudaStream_t st);
 // Edge-label ranks from d_etab[label - elo] when d_etab is set, else by binary

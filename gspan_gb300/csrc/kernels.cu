@@ -72,6 +72,7 @@ __device__ void hash_insert(uint32_t* table, uint32_t cap, uint32_t v, uint32_t*
 __device__ __forceinline__ void dom_insert(uint32_t* pool, const DomDesc& d, int p, uint32_t v, uint32_t* status)
 {
     uint32_t* base = pool + d.off + (uint64_t)p * d.cap;
+    v -= (uint32_t)d.vbase;   // ids local to the tuple's instance
     if (d.hash)
         hash_insert(base, d.cap, v, status);
     else
@@ -134,6 +135,34 @@ __global__ void k_label_presence(int32_t n, const int32_t* __restrict__ vlabels,
         eflag[(int64_t)edges[i].label - elo] = 1;
 }
 
+__device__ __forceinline__ int32_t last_at_most(const int64_t* base, int32_t n, int64_t x)
+{
+    int32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= x) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_batch_fixup(int32_t ninst, const int64_t* __restrict__ vbase, const int64_t* __restrict__ ebase,
+                              int32_t N, int32_t M, int32_t* __restrict__ offsets, gspan_edge* __restrict__ edges,
+                              uint32_t* status)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += stride)
+        offsets[v] += (int32_t)ebase[last_at_most(vbase, ninst, v)];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M; i += stride) {
+        const int32_t inst = last_at_most(ebase, ninst, i);
+        const int64_t nloc = vbase[inst + 1] - vbase[inst];
+        gspan_edge ed = edges[i];
+        if (ed.from < 0 || ed.from >= nloc || ed.to < 0 || ed.to >= nloc) atomicOr(status, kErrBadGraph);
+        ed.from += (int32_t)vbase[inst];
+        ed.to += (int32_t)vbase[inst];
+        edges[i] = ed;
+    }
+}
+
 __global__ void k_vertex_ranks(int32_t n, const int32_t* __restrict__ vlabels, int32_t vlo,
                                const int32_t* __restrict__ vtab, int32_t* __restrict__ vrank)
 {
@@ -178,7 +207,9 @@ constexpr int kSortBuckets = 128;
 // (edge label, to label, to) order in O(degree).  Input in any other order,
 // or a tuple space wider than kSortBuckets, falls back to ranking every entry
 // against its segment (O(degree^2), still stable).
-__global__ void __launch_bounds__(256) k_sort_segments(int32_t n, int32_t m, int32_t nvl, int32_t K,
+__global__ void __launch_bounds__(256) k_sort_segments(int32_t n, int32_t m, int32_t lwin, int32_t K,
+                                                       const int32_t* __restrict__ vrank,
+                                                       const int32_t* __restrict__ win_base,
                                                        const int32_t* __restrict__ offsets,
                                                        const gspan_edge* __restrict__ edges,
                                                        const uint64_t* __restrict__ keys, uint64_t* __restrict__ adj,
@@ -205,6 +236,10 @@ __global__ void __launch_bounds__(256) k_sort_segments(int32_t n, int32_t m, int
                 sorted &= pv.to < c.to || (pv.to == c.to && pv.label <= c.label);
             }
         }
+        // Counting sort needs every neighbour label inside the vertex's window.
+        const uint32_t wbase = (uint32_t)win_base[vrank[v]];
+        for (int32_t j = b + lane; j < e; j += 32)
+            sorted &= entry_tl(__ldg(keys + j)) - wbase < (uint32_t)lwin;
         sorted = __all_sync(kFull, sorted);
         if (!sorted || K > kSortBuckets) {
             for (int32_t j = b + lane; j < e; j += 32) {
@@ -218,11 +253,12 @@ __global__ void __launch_bounds__(256) k_sort_segments(int32_t n, int32_t m, int
             }
             continue;
         }
+        const uint32_t wb = wbase;
         for (int i = lane; i < kSortBuckets; i += 32) cnt[i] = 0;
         __syncwarp();
         for (int32_t j = b + lane; j < e; j += 32) {
             const uint64_t kj = __ldg(keys + j);
-            atomicAdd(&cnt[entry_el(kj) * (uint32_t)nvl + entry_tl(kj)], 1u);
+            atomicAdd(&cnt[entry_el(kj) * (uint32_t)lwin + entry_tl(kj) - wb], 1u);
         }
         __syncwarp();
         // Exclusive scan of the bucket counts; lane i owns buckets 4i .. 4i+3.
@@ -253,7 +289,7 @@ __global__ void __launch_bounds__(256) k_sort_segments(int32_t n, int32_t m, int
             uint32_t bucket = 0;
             if (valid) {
                 kj = __ldg(keys + j);
-                bucket = entry_el(kj) * (uint32_t)nvl + entry_tl(kj);
+                bucket = entry_el(kj) * (uint32_t)lwin + entry_tl(kj) - wb;
             }
             const unsigned vm = __ballot_sync(kFull, valid);
             unsigned peers = 0;
@@ -273,21 +309,22 @@ __global__ void __launch_bounds__(256) k_sort_segments(int32_t n, int32_t m, int
 // the 1-edge code (0,1,label(u),edge label,label(w)).
 
 __device__ __forceinline__ bool seed_key(const int32_t* __restrict__ src, const uint64_t* __restrict__ adj,
-                                         const int32_t* __restrict__ vrank, int32_t nvl, int32_t nel, int64_t i,
-                                         int32_t* key, uint32_t* u, uint32_t* w)
+                                         const int32_t* __restrict__ vrank, const int32_t* __restrict__ win_base,
+                                         int32_t lwin, int32_t nel, int64_t i, int32_t* key, uint32_t* u, uint32_t* w)
 {
     const uint64_t e = adj[i];
     *u = (uint32_t)src[i];
     *w = entry_to(e);
     const int32_t fl = vrank[*u];
     const int32_t tl = (int32_t)entry_tl(e);
-    *key = (fl * nel + (int32_t)entry_el(e)) * nvl + tl;
-    return fl <= tl;
+    const int32_t local = tl - win_base[fl];
+    *key = (fl * nel + (int32_t)entry_el(e)) * lwin + local;
+    return fl <= tl && (uint32_t)local < (uint32_t)lwin;
 }
 
 __global__ void k_seed_count(int32_t m, const int32_t* __restrict__ src, const uint64_t* __restrict__ adj,
-                             const int32_t* __restrict__ vrank, int32_t nvl, int32_t nel,
-                             unsigned long long* __restrict__ counts)
+                             const int32_t* __restrict__ vrank, const int32_t* __restrict__ win_base, int32_t lwin,
+                             int32_t nel, unsigned long long* __restrict__ counts)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -296,7 +333,7 @@ __global__ void k_seed_count(int32_t m, const int32_t* __restrict__ src, const u
         const int64_t i = base + lane;
         int32_t key = 0;
         uint32_t u, w;
-        const bool ok = i < m && seed_key(src, adj, vrank, nvl, nel, i, &key, &u, &w);
+        const bool ok = i < m && seed_key(src, adj, vrank, win_base, lwin, nel, i, &key, &u, &w);
         const unsigned mask = __ballot_sync(kFull, ok);
         if (ok) {
             const unsigned peers = __match_any_sync(mask, key);
@@ -306,7 +343,8 @@ __global__ void k_seed_count(int32_t m, const int32_t* __restrict__ src, const u
 }
 
 __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const uint64_t* __restrict__ adj,
-                               const int32_t* __restrict__ vrank, int32_t nvl, int32_t nel, LevelKeys keys,
+                               const int32_t* __restrict__ vrank, const int32_t* __restrict__ win_base,
+                               int32_t lwin, int32_t nel, LevelKeys keys,
                                uint32_t* __restrict__ pool, int32_t* __restrict__ col0, int32_t* __restrict__ col1,
                                uint32_t* status)
 {
@@ -317,7 +355,7 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
         const int64_t i = base + lane;
         int32_t key = 0;
         uint32_t u = 0, w = 0;
-        bool ok = i < m && seed_key(src, adj, vrank, nvl, nel, i, &key, &u, &w);
+        bool ok = i < m && seed_key(src, adj, vrank, win_base, lwin, nel, i, &key, &u, &w);
         const int32_t a = ok ? keys.act[key] : -1;
         ok = a >= 0;
         if (ok) {
@@ -351,7 +389,7 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
 struct ExpandDev {
     const int32_t* offsets;
     const uint64_t* adj;
-    int32_t nvl, nel;
+    int32_t nvl, nel, lwin;
     const ParentMeta* parents;
     int32_t nparents;
     int64_t ntiles;
@@ -377,7 +415,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WarpScratch& W = reinterpret_cast<WarpScratch*>(smem_raw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
-    const int32_t LeLv = a.nel * a.nvl;
+    const int32_t LeLv = a.nel * a.lwin;
 
     for (;;) {
         long long tile = 0;
@@ -413,7 +451,8 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                 const int32_t u = W.img[lane][P.src_v[sq]];
                 const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
                 if (segs) {
-                    const uint32_t el = P.mseg_kc[q] / (uint32_t)a.nvl, tl = P.mseg_kc[q] % (uint32_t)a.nvl;
+                    const uint32_t el = P.mseg_kc[q] / (uint32_t)a.lwin;
+                    const uint32_t tl = (uint32_t)P.lbase + P.mseg_kc[q] % (uint32_t)a.lwin;
                     st = lower_bound_entry(a.adj, b, e, pack_entry(el, tl, 0));
                     c = lower_bound_entry(a.adj, st, e, pack_entry(el, tl + 1, 0)) - st;
                 } else {
@@ -522,10 +561,10 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                 const uint64_t e = __ldg(a.adj + W.start[owner][s] + j);
                 to = entry_to(e);
                 const int32_t tl = (int32_t)entry_tl(e);
-                bool fresh = tl >= min_label;
+                bool fresh = tl >= min_label && (uint32_t)(tl - P.lbase) < (uint32_t)a.lwin;
                 for (int p = 0; p < nv; ++p) fresh &= W.img[owner][p] != (int32_t)to;
                 ok = fresh;
-                key = key_base + (segs ? P.mseg_s[s] : s) * LeLv + (int32_t)entry_el(e) * a.nvl + tl;
+                key = key_base + (segs ? P.mseg_s[s] : s) * LeLv + (int32_t)entry_el(e) * a.lwin + (tl - P.lbase);
             }
             const unsigned mask = __ballot_sync(kFull, ok);
             if (kPass == Pass::Count) {
@@ -600,7 +639,7 @@ struct MaskDev {
     const uint32_t* segmask;
     const uint32_t* selfloop;
     bool symmetric;
-    int32_t n, m, nvl, nel, mw;
+    int32_t n, m, nvl, nel, mw, lwin;
     const ParentMeta* parents;
     int32_t nparents;
     int64_t ntiles;
@@ -636,6 +675,8 @@ __device__ __forceinline__ void add_fresh_bits(uint32_t fresh, uint32_t* sizes, 
                                                int lane)
 {
     if (!__any_sync(kFull, fresh)) return;
+    // An image seen for the first time brings most of its tuple bits at once,
+    // so transpose all 32 bits and let lane b add bit b's count.
     uint32_t mine = 0;
     for (int b = 0; b < 32; ++b) {
         const uint32_t c = __popc(__ballot_sync(kFull, (fresh >> b) & 1u));
@@ -644,7 +685,8 @@ __device__ __forceinline__ void add_fresh_bits(uint32_t fresh, uint32_t* sizes, 
     if (mine) atomicAdd(sizes + out + (int64_t)(word * 32 + lane) * stride, mine);
 }
 
-__global__ void k_segmask(int32_t n, int32_t nvl, int32_t segw, const int32_t* __restrict__ offsets,
+__global__ void k_segmask(int32_t n, int32_t lwin, int32_t segw, const int32_t* __restrict__ vrank,
+                          const int32_t* __restrict__ win_base, const int32_t* __restrict__ offsets,
                           const uint64_t* __restrict__ adj, uint32_t* __restrict__ segmask)
 {
     const int lane = threadIdx.x & 31;
@@ -652,9 +694,10 @@ __global__ void k_segmask(int32_t n, int32_t nvl, int32_t segw, const int32_t* _
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t v = warp; v < n; v += nwarps) {
         uint32_t w[kMaxMaskWords] = {0, 0, 0, 0};
+        const uint32_t wb = (uint32_t)win_base[vrank[v]];
         for (int32_t j = offsets[v] + lane; j < offsets[v + 1]; j += 32) {
             const uint64_t ent = adj[j];
-            const uint32_t kc = entry_el(ent) * (uint32_t)nvl + entry_tl(ent);
+            const uint32_t kc = entry_el(ent) * (uint32_t)lwin + entry_tl(ent) - wb;
 #pragma unroll
             for (int i = 0; i < kMaxMaskWords; ++i) w[i] |= (uint32_t)(i == (int)(kc >> 5)) << (kc & 31u);
         }
@@ -706,7 +749,7 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
     int32_t (*img_all)[kMaxV + 1] = img_s[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     int32_t* img = img_all[lane];
-    const int32_t K = a.nel * a.nvl;
+    const int32_t K = a.nel * a.lwin;
     const int mw = a.mw;
 
     for (;;) {
@@ -728,7 +771,7 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
             if (live) {
                 const unsigned peers = __match_any_sync(lm, u);
                 if (lane == __ffs(peers) - 1)
-                    first_row = atomicAdd(a.R + P.r_off + (int64_t)s * a.n + u, (uint32_t)__popc(peers)) == 0;
+                    first_row = atomicAdd(a.R + P.r_off + (int64_t)s * P.nloc + (u - P.vbase), (uint32_t)__popc(peers)) == 0;
             }
             // One append per warp for the source images seen for the first time.
             const unsigned fm = __ballot_sync(kFull, first_row);
@@ -750,7 +793,8 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
             const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
             const uint64_t lo = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
                                        : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
-            uint32_t* Hs = a.H + P.h_off + (int64_t)s * a.m;
+            // H of this source, indexed by batch-wide entry index.
+            uint32_t* Hs = a.H + P.h_off + (int64_t)s * P.mloc - P.ebase;
             uint32_t ex[kMaxMaskWords] = {0, 0, 0, 0};
             for (int el = 0; el < a.nel; ++el) {
                 for (int i = 0; i < nv; ++i) {
@@ -800,7 +844,7 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                         const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
                         const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
                         if (first && last && maxub - minlb == hits) {
-                            const uint32_t kc = (uint32_t)(el * a.nvl + t);
+                            const uint32_t kc = (uint32_t)(el * a.lwin + t - P.lbase);
 #pragma unroll
                             for (int w = 0; w < kMaxMaskWords; ++w)
                                 ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
@@ -813,7 +857,7 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                 mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
             }
             for (int p = 0; p < nv; ++p) {
-                uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * a.n + (live ? img[p] : 0)) * mw;
+                uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * P.nloc + (live ? img[p] - P.vbase : 0)) * mw;
                 const int64_t out = P.sz_off + (int64_t)s * K * (nv + 1) + p;
                 for (int w = 0; w < mw; ++w) add_fresh_bits(or_fresh(rowm + w, mk[w]), a.sizes, out, nv + 1, w, lane);
             }
@@ -856,7 +900,8 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                 const int64_t out = P.sz_off + (int64_t)nsrc * K * (nv + 1);
                 for (int p = 0; p < nv; ++p) {
                     const uint32_t got =
-                        ok ? or_fresh(a.MB + P.b_off + ((int64_t)p * a.n + img[p]) * P.bw + (bk >> 5), 1u << (bk & 31))
+                        ok ? or_fresh(a.MB + P.b_off + ((int64_t)p * P.nloc + (img[p] - P.vbase)) * P.bw + (bk >> 5),
+                                      1u << (bk & 31))
                            : 0u;
                     for (int w = 0; w < P.bw; ++w)
                         add_fresh_bits((bk >> 5) == w ? got : 0u, a.sizes, out + p, nv, w, lane);
@@ -887,7 +932,7 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int32_t K = a.nel * a.nvl;
+    const int32_t K = a.nel * a.lwin;
     const int mw = a.mw;
     const unsigned long long total = a.tprefix[a.nps];
     unsigned long long scanned = 0;
@@ -902,7 +947,7 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
         const int64_t idx = (int64_t)(task - a.tprefix[lo]);
         if (idx >= P.t_cap) continue;   // the row pass flagged an overflow; never read past the list
         const int32_t u = a.touched[P.t_off + (int64_t)s * P.t_cap + idx];
-        uint32_t* Ru = a.R + P.r_off + (int64_t)s * a.n + u;
+        uint32_t* Ru = a.R + P.r_off + (int64_t)s * P.nloc + (u - P.vbase);
         const uint32_t r = *Ru;
         __syncwarp();
         const int min_label = P.min_label;
@@ -910,8 +955,8 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
         const uint64_t lo_key = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
                                        : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
         const int32_t st = lower_bound_entry(a.adj, b, e, lo_key);
-        uint32_t* Hs = a.H + P.h_off + (int64_t)s * a.m;
-        uint32_t* NM = a.M + P.m_off + ((int64_t)s * (P.nv + 1) + P.nv) * a.n * mw;
+        uint32_t* Hs = a.H + P.h_off + (int64_t)s * P.mloc - P.ebase;
+        uint32_t* NM = a.M + P.m_off + ((int64_t)s * (P.nv + 1) + P.nv) * P.nloc * mw;
         const int64_t nm_out = P.sz_off + (int64_t)s * K * (P.nv + 1) + P.nv;
         unsigned long long* cnt = a.counts + P.key_base + (int64_t)s * K;
         scanned += (unsigned long long)(e - st);
@@ -923,8 +968,8 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
             if (i < e) {
                 const uint64_t ent = __ldg(a.adj + i);
                 const int32_t tl = (int32_t)entry_tl(ent);
-                ok = tl >= min_label;
-                kc = (int32_t)entry_el(ent) * a.nvl + tl;
+                ok = tl >= min_label && (uint32_t)(tl - P.lbase) < (uint32_t)a.lwin;
+                kc = (int32_t)entry_el(ent) * a.lwin + tl - P.lbase;
                 to = entry_to(ent);
                 const uint32_t h = Hs[i];
                 if (h) Hs[i] = 0u;
@@ -941,7 +986,7 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
             }
             const int32_t nk = __shfl_down_sync(kFull, segk, 1);
             if (ok && (lane == 31 || nk != segk) && v) atomicAdd(cnt + kc, v);
-            const bool fresh = ok && diff > 0 && or_fresh(NM + (int64_t)to * mw + (kc >> 5), 1u << (kc & 31));
+            const bool fresh = ok && diff > 0 && or_fresh(NM + (int64_t)(to - P.vbase) * mw + (kc >> 5), 1u << (kc & 31));
             const unsigned fmask = __ballot_sync(kFull, fresh);
             if (fresh) {
                 const unsigned peers = __match_any_sync(fmask, kc);
@@ -1010,6 +1055,15 @@ cudaError_t launch_label_presence(int32_t n, const int32_t* d_vlabels, int32_t v
     return cudaGetLastError();
 }
 
+cudaError_t launch_batch_fixup(int32_t ninst, const int64_t* d_vbase, const int64_t* d_ebase, int32_t N, int32_t M,
+                               int32_t* d_offsets, gspan_edge* d_edges, uint32_t* d_status, cudaStream_t st)
+{
+    if (N == 0 && M == 0) return cudaSuccess;
+    k_batch_fixup<<<grid_for(std::max<int64_t>(N, M), 256), 256, 0, st>>>(ninst, d_vbase, d_ebase, N, M, d_offsets,
+                                                                          d_edges, d_status);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_vertex_ranks(int32_t n, const int32_t* d_vlabels, int32_t vlo, const int32_t* d_vtab,
                                 int32_t* d_vrank, cudaStream_t st)
 {
@@ -1027,8 +1081,8 @@ cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d
                                                          g.nel, d_tmp, d_status);
     }
     if (g.n > 0) {
-        k_sort_segments<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, g.nvl, g.nel * g.nvl, d_offsets,
-                                                                          d_edges, d_tmp, g.adj, g.src, d_status);
+        k_sort_segments<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(
+            g.n, g.m, g.lwin, g.nel * g.lwin, g.vrank, g.win_base, d_offsets, d_edges, d_tmp, g.adj, g.src, d_status);
     }
     return cudaGetLastError();
 }
@@ -1036,7 +1090,7 @@ cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d
 cudaError_t launch_seed_count(const DevGraph& g, unsigned long long* counts, cudaStream_t st)
 {
     if (g.m == 0) return cudaSuccess;
-    k_seed_count<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.nvl, g.nel, counts);
+    k_seed_count<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.win_base, g.lwin, g.nel, counts);
     return cudaGetLastError();
 }
 
@@ -1044,7 +1098,7 @@ cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* poo
                                 uint32_t* status, cudaStream_t st)
 {
     if (g.m == 0) return cudaSuccess;
-    k_seed_support<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.nvl, g.nel, keys, pool,
+    k_seed_support<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.win_base, g.lwin, g.nel, keys, pool,
                                                        col0, col1, status);
     return cudaGetLastError();
 }
@@ -1070,6 +1124,7 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     a.adj = x.g->adj;
     a.nvl = x.g->nvl;
     a.nel = x.g->nel;
+    a.lwin = x.g->lwin;
     a.parents = x.parents;
     a.nparents = x.nparents;
     a.ntiles = x.ntiles;
@@ -1106,7 +1161,8 @@ cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st)
 cudaError_t launch_segmask(DevGraph& g, cudaStream_t st)
 {
     if (g.n == 0 || g.segw == 0) return cudaSuccess;
-    k_segmask<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.nvl, g.segw, g.offsets, g.adj, g.segmask);
+    k_segmask<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.lwin, g.segw, g.vrank, g.win_base, g.offsets,
+                                                                 g.adj, g.segmask);
     return cudaGetLastError();
 }
 
@@ -1124,6 +1180,7 @@ MaskDev mask_dev(const MaskArgs& x)
     a.nvl = x.g->nvl;
     a.nel = x.g->nel;
     a.mw = x.g->segw;
+    a.lwin = x.g->lwin;
     a.parents = x.parents;
     a.nparents = x.nparents;
     a.ntiles = x.ntiles;

@@ -120,6 +120,7 @@ struct Parent {
 struct Found {
     std::vector<CodeEdge> code;
     int support;
+    int inst;      // mining instance (0 for a single graph)
 };
 
 struct Active {
@@ -127,6 +128,8 @@ struct Active {
     std::vector<CodeEdge> code;
     uint64_t count;       // embeddings of this child
     int nvc;              // pattern vertices of the child
+    int32_t vbase = 0;    // the child's instance: first vertex and vertex count
+    int32_t nloc = 0;
 };
 
 std::vector<int> rightmost_path(const std::vector<CodeEdge>& c)
@@ -174,9 +177,29 @@ struct Run {
     gspan_ctx* ctx;
     const DevGraph& g;
     int k;
-    int min_support;
-    uint64_t threshold;   // embedding count an active tuple needs
+    const std::vector<int32_t>& minsup;   // per mining instance
     gspan_stats st{};
+
+    // A pattern's instance follows from any of its labels (the first one's).
+    int instance_of(int fl) const { return g.label_instance.empty() ? 0 : g.label_instance[fl]; }
+    int min_support_of(int fl) const { return minsup[instance_of(fl)]; }
+    // Embeddings a child needs before its support is worth counting: MNI
+    // support never exceeds the embedding count.
+    uint64_t threshold(int fl) const { return (uint64_t)std::max(min_support_of(fl), 1); }
+    // Vertex and entry ranges of the instance a pattern (first label fl) lives in.
+    void window(int fl, int32_t* vbase, int32_t* nloc, int32_t* ebase, int32_t* mloc) const
+    {
+        const int i = instance_of(fl);
+        *vbase = (int32_t)g.inst_vbase[i];
+        *nloc = (int32_t)(g.inst_vbase[i + 1] - g.inst_vbase[i]);
+        *ebase = (int32_t)g.inst_ebase[i];
+        *mloc = (int32_t)(g.inst_ebase[i + 1] - g.inst_ebase[i]);
+    }
+    void place(Active& a) const
+    {
+        int32_t eb, ml;
+        window(a.code[0].fl, &a.vbase, &a.nloc, &eb, &ml);
+    }
     std::vector<Found> found;
     cudaStream_t s;
     bool profile;
@@ -189,13 +212,13 @@ struct Run {
         return cudaMemcpyAsync(dst, src, bytes, kind, strm);
     }
 
-    bool use_hash(uint64_t count) const
+    bool use_hash(uint64_t count, int32_t nloc) const
     {
         const int mode = ctx->opts.domain_mode;
         if (mode == 1) return false;
         if (mode == 2) return true;
         const double thr = ctx->opts.hash_threshold > 0 ? ctx->opts.hash_threshold : 1.0;
-        return 64.0 * (double)std::min<uint64_t>(count, (uint64_t)g.n) < (double)g.n * thr;
+        return 64.0 * (double)std::min<uint64_t>(count, (uint64_t)nloc) < (double)nloc * thr;
     }
 
     // Domains, act[] and output rows for the active tuples; allocates `out`
@@ -206,16 +229,19 @@ struct Run {
         as.nact = (int32_t)act.size();
         as.dom.resize(act.size());
         as.mat.assign(act.size(), -1);
-        const uint32_t words = (uint32_t)std::max<int64_t>(1, ((int64_t)g.n + 31) / 32);
+
         uint64_t bitmap_words = 0, hash_words = 0;
         int out_cols = 0;
         int64_t out_rows = 0;
         for (size_t i = 0; i < act.size(); ++i) {
-            const bool h = use_hash(act[i].count);
+            const int32_t nloc = act[i].nloc;
+            const bool h = use_hash(act[i].count, nloc);
+            const uint32_t words = (uint32_t)std::max<int64_t>(1, ((int64_t)nloc + 31) / 32);
             DomDesc d{};
             d.nvc = (uint16_t)act[i].nvc;
             d.hash = h ? 1 : 0;
-            d.cap = h ? next_pow2(2 * std::min<uint64_t>(act[i].count, (uint64_t)g.n)) : words;
+            d.vbase = act[i].vbase;
+            d.cap = h ? next_pow2(2 * std::min<uint64_t>(act[i].count, (uint64_t)nloc)) : words;
             if (h) {
                 d.off = hash_words;
                 hash_words += (uint64_t)d.cap * d.nvc;
@@ -304,7 +330,7 @@ struct Run {
 
     gspan_status seeds(std::vector<Parent>& next, Table& table)
     {
-        const int64_t nkeys = (int64_t)g.nvl * g.nel * g.nvl;
+        const int64_t nkeys = (int64_t)g.nvl * g.nel * g.lwin;
         if (nkeys > (int64_t)std::numeric_limits<int32_t>::max())
             return fail(ctx, GSPAN_ERR_LIMIT, "too many distinct labels for the 1-edge key space");
         if (g.m == 0 || nkeys == 0) return GSPAN_OK;
@@ -322,11 +348,12 @@ struct Run {
             const uint64_t c = counts[key];
             if (c == 0) continue;
             st.seeds += c;
-            if (c < threshold) continue;
-            const int fl = (int)(key / ((int64_t)g.nel * g.nvl));
-            const int el = (int)((key / g.nvl) % g.nel);
-            const int tl = (int)(key % g.nvl);
+            const int fl = (int)(key / ((int64_t)g.nel * g.lwin));
+            const int el = (int)((key / g.lwin) % g.nel);
+            const int tl = g.win_base_h[fl] + (int)(key % g.lwin);
+            if (c < threshold(fl)) continue;
             act.push_back(Active{(int32_t)key, {CodeEdge{0, 1, fl, el, tl}}, c, 2});
+            place(act.back());
         }
         ActiveSet as;
         const bool mat = k > 1;
@@ -349,8 +376,8 @@ struct Run {
             st.seed_ms += ms;
         }
         for (int32_t a = 0; a < as.nact; ++a) {
-            if (sup[a] < min_support) continue;
-            found.push_back(Found{act[a].code, sup[a]});
+            if (sup[a] < min_support_of(act[a].code[0].fl)) continue;
+            found.push_back(Found{act[a].code, sup[a], instance_of(act[a].code[0].fl)});
             if (k > 1) next.push_back(Parent{act[a].code, as.mat[a], as.mat[a] + (int64_t)act[a].count});
         }
         as.release(s);
@@ -413,7 +440,7 @@ struct Run {
 
     gspan_status level(int size, std::vector<Parent>& parents, Table& table, std::vector<Parent>& next, Table& out)
     {
-        const int32_t K = g.nel * g.nvl;
+        const int32_t K = g.nel * g.lwin;
         const int np = (int)parents.size();
         const int mode = ctx->opts.path;
         const bool mask_possible = g.segw > 0 && mode != 1;
@@ -431,6 +458,8 @@ struct Run {
             P.nv = (int16_t)nv;
             P.vn = (int16_t)c[rm[0]].to;
             P.min_label = (int16_t)c[0].fl;
+            P.lbase = g.win_base_h[c[0].fl];
+            window(c[0].fl, &P.vbase, &P.nloc, &P.ebase, &P.mloc);
             P.vlab[0] = (int16_t)c[0].fl;
             for (const CodeEdge& e : c)
                 if (e.from < e.to) P.vlab[e.to] = (int16_t)e.tl;
@@ -479,7 +508,7 @@ struct Run {
                 const int lo_el = s2 == 0 ? 0 : P.src_el[s2];
                 const int lo_tl = s2 == 0 ? P.min_label : P.src_tl[s2];
                 for (int32_t kc = 0; kc < K && kc < 32 * kMaxMaskWords; ++kc) {
-                    const int el = kc / g.nvl, tl = kc % g.nvl;
+                    const int el = kc / g.lwin, tl = P.lbase + kc % g.lwin;
                     if (tl >= P.min_label && (el > lo_el || (el == lo_el && tl >= lo_tl)))
                         P.range[s2][kc >> 5] |= 1u << (kc & 31);
                 }
@@ -490,7 +519,7 @@ struct Run {
                 // zero by its sweep); the per-candidate path examines about
                 // rows x sources x (mean degree behind an embedding's vertex)
                 // candidates, each far dearer than clearing a word.
-                const double clear_words = (double)P.nsrc * (nv + 1) * g.n * g.segw + (double)nv * g.n * P.bw;
+                const double clear_words = (double)P.nsrc * (nv + 1) * P.nloc * g.segw + (double)nv * P.nloc * P.bw;
                 use_mask[i] = mode == 2 || (double)rows * P.nsrc * g.edge_biased_degree > 0.125 * clear_words;
             }
         }
@@ -526,9 +555,9 @@ struct Run {
                 continue;
             }
             ParentMeta P = meta[i];
-            const int64_t t_cap = std::min<int64_t>(rows, g.n);
-            const int64_t rw = (int64_t)P.nsrc * g.n, hw = (int64_t)P.nsrc * g.m;
-            const int64_t mw2 = (int64_t)P.nsrc * (P.nv + 1) * g.n * g.segw, bw2 = (int64_t)P.nv * g.n * P.bw;
+            const int64_t t_cap = std::max<int64_t>(1, std::min<int64_t>(rows, P.nloc));
+            const int64_t rw = (int64_t)P.nsrc * P.nloc, hw = (int64_t)P.nsrc * P.mloc;
+            const int64_t mw2 = (int64_t)P.nsrc * (P.nv + 1) * P.nloc * g.segw, bw2 = (int64_t)P.nv * P.nloc * P.bw;
             const int64_t tw = (int64_t)P.nsrc * t_cap;
             const double bytes = 4.0 * (double)(rw + hw + mw2 + bw2 + tw);
             if (groups.empty() || (!groups.back().metas.empty() && groups.back().bytes + bytes > budget))
@@ -711,15 +740,15 @@ struct Run {
                 const uint64_t cnt = counts[key];
                 if (cnt == 0) continue;
                 st.extended += cnt;
-                if (cnt < threshold) continue;
+                if (cnt < threshold(c[0].fl)) continue;
                 std::vector<CodeEdge> child = c;
                 int nvc;
                 int64_t size_at;
                 int stride;
                 if (lk < (int64_t)P.nsrc * K) {
                     const int s2 = (int)(lk / K);
-                    const int el = (int)((lk % K) / g.nvl);
-                    const int tl = (int)(lk % g.nvl);
+                    const int el = (int)((lk % K) / g.lwin);
+                    const int tl = P.lbase + (int)(lk % g.lwin);
                     child.push_back(CodeEdge{P.src_v[s2], P.nv, -1, el, tl});
                     nvc = P.nv + 1;
                     size_at = sz_off[i] + lk * (P.nv + 1);
@@ -742,9 +771,9 @@ struct Run {
                     }
                     const int sup = (int)std::min<uint32_t>(best, 0x7fffffffu);
                     ++st.support_keys;
-                    if (sup >= min_support) freq.push_back(Freq{key, std::move(child), cnt, nvc, sup});
+                    if (sup >= min_support_of(c[0].fl)) freq.push_back(Freq{key, std::move(child), cnt, nvc, sup});
                 } else {
-                    cand_act.push_back(Active{key, std::move(child), cnt, nvc});
+                    cand_act.push_back(Active{key, std::move(child), cnt, nvc, P.vbase, P.nloc});
                 }
             }
         }
@@ -775,12 +804,16 @@ struct Run {
             as.release(s);
             if (rc != GSPAN_OK) return rc;
             for (size_t a2 = 0; a2 < cand_act.size(); ++a2)
-                if (sup[a2] >= min_support)
+                if (sup[a2] >= min_support_of(cand_act[a2].code[0].fl))
                     freq.push_back(Freq{cand_act[a2].key, std::move(cand_act[a2].code), cand_act[a2].count,
                                         cand_act[a2].nvc, sup[a2]});
         }
 
-        for (const Freq& f : freq) found.push_back(Found{f.code, f.support});
+        st.frontier_rows = 0;
+        for (const Freq& f : freq) {
+            found.push_back(Found{f.code, f.support, instance_of(f.code[0].fl)});
+            st.frontier_rows += f.count;
+        }
         if (size + 1 >= k || freq.empty()) return GSPAN_OK;
 
         // Materialise the frequent children, grouped by tuple (offsets from the
@@ -872,7 +905,7 @@ struct Run {
 
 }  // namespace
 
-gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, int min_support, gspan_emit_fn emit, void* user,
+gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<int32_t>& minsup, const EmitFn& emit,
                   gspan_stats* stats)
 {
     const auto t0 = Clock::now();
@@ -880,7 +913,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, int min_support, gsp
     // set-up); here it is an argument error.
     if (k < 1) return fail(ctx, GSPAN_ERR_INVALID, "k must be at least 1");
     if (k > kMaxE) return fail(ctx, GSPAN_ERR_LIMIT, "k exceeds the largest supported pattern size");
-    Run run{ctx, g, k, min_support, (uint64_t)std::max(min_support, 1)};
+    Run run{ctx, g, k, minsup};
     run.s = ctx->stream;
     run.profile = ctx->opts.profile != 0;
     GS_CK(cudaMemsetAsync(ctx->d_status, 0, 4, run.s), "clear status");
@@ -928,7 +961,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, int min_support, gsp
                 buf[j].edge_label = e.el < 0 ? -1 : g.elabel_of_rank[e.el];
                 buf[j].to_label = e.tl < 0 ? -1 : g.vlabel_of_rank[e.tl];
             }
-            if (emit(user, buf.data(), (int32_t)buf.size(), f.support) != 0)
+            if (emit(f.inst, buf.data(), (int32_t)buf.size(), f.support) != 0)
                 return fail(ctx, GSPAN_ERR_ABORTED, "stopped by the emit callback");
         }
     }

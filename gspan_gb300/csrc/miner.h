@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -47,8 +48,17 @@ struct gspan_graph {
 };
 
 namespace gs {
-gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, int min_support, gspan_emit_fn emit, void* user,
+// Receives (instance, code, length, support) in pre-order, instance by instance.
+using EmitFn = std::function<int(int, const gspan_pattern_edge*, int32_t, int32_t)>;
+// Mines every instance of `g` (one for a single graph) with its own minimum
+// support minsup[instance].
+gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<int32_t>& minsup, const EmitFn& emit,
                   gspan_stats* stats);
 gspan_status fail(gspan_ctx* ctx, gspan_status s, const std::string& msg);
+// Builds the device store from `ninst` host CSR graphs (graph_store.cc).
+gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, const int32_t* ms,
+                           const int32_t* const* offs, const int32_t* const* vls, const gspan_edge* const* eds,
+                           gspan_graph** out);
+void free_graph(gspan_graph* gr, cudaStream_t st);
 gspan_status cuda_fail(gspan_ctx* ctx, cudaError_t e, const char* what);
 }  // namespace gs

@@ -96,8 +96,18 @@ def csr_from_edge_list(n: int, vlabels: np.ndarray, eu: np.ndarray, ev: np.ndarr
     frm = np.concatenate([eu, ev])
     to = np.concatenate([ev, eu])
     lab = np.concatenate([el, el])
-    order = np.lexsort((lab, to, frm))
-    frm, to, lab = frm[order], to[order], lab[order]
+    lmin = int(lab.min()) if lab.size else 0
+    lbits = max(1, int(lab.max() - lmin).bit_length()) if lab.size else 1
+    if frm.size and n > 0 and (2 * math.log2(n) + lbits) < 62:
+        # One packed key (from, to, label) sorts in a single pass.
+        key = ((frm * n + to) << lbits) | (lab - lmin)
+        key.sort()
+        lab = (key & ((1 << lbits) - 1)) + lmin
+        ft = key >> lbits
+        frm, to = ft // n, ft % n
+    else:
+        order = np.lexsort((lab, to, frm))
+        frm, to, lab = frm[order], to[order], lab[order]
     deg = np.bincount(frm, minlength=n) if n else np.zeros(0, dtype=np.int64)
     offsets = np.zeros(n + 1, dtype=np.int64)
     np.cumsum(deg, out=offsets[1:])
@@ -246,3 +256,20 @@ def chung_lu_3_7m(seed: int = 3) -> CSR:
     sqrt(2m), 37 vertex labels Zipf(0.8), 1 edge label."""
     m = 16_500_000
     return chung_lu(3_700_000, m, 2.3, 37, 0.8, seed, max_deg=math.sqrt(2 * m))
+
+
+def batch_instances(seed: int = 2, count: int = 256) -> tuple[list[CSR], list[int]]:
+    """Independent mining instances: Chung-Lu graphs with n log-uniform in
+    [1,000, 200,000], average degree uniform in [4, 24], 8 to 32 vertex labels
+    Zipf(1.0), exponent 2.1, degree cap sqrt(2m), 1 edge label.  Returns the
+    graphs and their min supports (2 % of n)."""
+    u = rand_unit(seed, 21, 0, count * 3).reshape(count, 3)
+    graphs, sups = [], []
+    lo, hi = math.log(1000.0), math.log(200000.0)
+    for i in range(count):
+        n = int(round(math.exp(lo + u[i, 0] * (hi - lo))))
+        m = int(round(n * (4.0 + 20.0 * u[i, 1]) / 2.0))
+        nlabels = 8 + min(24, int(u[i, 2] * 25))
+        graphs.append(chung_lu(n, m, 2.1, nlabels, 1.0, seed * 1000003 + i, max_deg=math.sqrt(2.0 * m)))
+        sups.append(int(0.02 * n))
+    return graphs, sups

@@ -76,6 +76,7 @@ typedef struct gspan_stats {
     double mine_ms;              /* host wall time of gspan_mine */
     uint64_t h2d_bytes;          /* host->device bytes copied by gspan_mine */
     uint64_t d2h_bytes;          /* device->host bytes copied by gspan_mine */
+    uint64_t frontier_rows;      /* embeddings of the frequent patterns of the deepest level mined */
     uint64_t mask_parents;       /* parent patterns extended by the mask kernels */
     uint64_t candidate_parents;  /* parent patterns extended by the per-candidate kernels */
     /* Per kernel family: launches, algorithmic bytes, and (profile == 1 only)
@@ -123,6 +124,31 @@ gspan_status gspan_graph_free(gspan_ctx* ctx, gspan_graph* graph);
  * LIMIT.  `stats` may be NULL. */
 gspan_status gspan_mine(gspan_ctx* ctx, const gspan_graph* graph, int32_t k, int32_t min_support,
                         gspan_emit_fn emit, void* user, gspan_stats* stats);
+
+/* ---- Batches: many independent mining instances in one device store ----
+ * No counterpart in the reference, which mines one graph per process.  Each
+ * instance is a separate CSR graph (vertex ids local to it); its results are
+ * exactly those of gspan_mine on that graph alone with its own min_support,
+ * while every extension level of all instances runs in the same kernel
+ * launches.  Vertex labels are ranked per instance, so all instances together
+ * may hold at most 65535 distinct (instance, label) pairs. */
+typedef int (*gspan_batch_emit_fn)(void* user, int32_t instance, const gspan_pattern_edge* code, int32_t len,
+                                   int32_t support);
+
+/* Uploads `ninst` graphs (arrays per instance, layout as gspan_graph_upload).
+ * An edge whose ends are outside its own instance returns INVALID. */
+gspan_status gspan_batch_upload(gspan_ctx* ctx, int32_t ninst, const int32_t* nr_nodes, const int32_t* nr_edges,
+                                const int32_t* const* offsets, const int32_t* const* vlabels,
+                                const gspan_edge* const* edges, gspan_graph** out);
+
+/* Mines every instance of a batch with min_support[instance]; emits instance
+ * by instance (ascending), each in the reference's pre-order.  gspan_mine on
+ * a batch of more than one instance returns INVALID. */
+gspan_status gspan_mine_batch(gspan_ctx* ctx, const gspan_graph* batch, int32_t k, const int32_t* min_support,
+                              gspan_batch_emit_fn emit, void* user, gspan_stats* stats);
+
+/* Number of instances in an uploaded graph (1 for gspan_graph_upload). */
+int32_t gspan_graph_instances(const gspan_graph* graph);
 
 /* MNI support of an embedding table in device memory (the reference's
  * support_gpu, gspan.cu:200-289, for a column table): `cols` is a host array
