@@ -66,6 +66,13 @@ struct DevGraph {
     // Every entry u->x with edge label l has a reverse entry x->u with label l
     // (checked at upload; true for every graph built by the text loader).
     bool symmetric = false;
+    // rev[e]: index of the reverse entry of e (the k-th of a run of equal
+    // entries pairs with the k-th of the reverse run); built with the symmetry
+    // check.  When the graph is symmetric and has one edge label, level tables
+    // also carry each pattern edge's entry index (entry_cols), which replaces
+    // most adjacency searches of the mask row pass.
+    int32_t* rev = nullptr;
+    bool entry_cols = false;
     // Mean degree of a vertex reached through an edge (sum d^2 / sum d): the
     // expected adjacency length behind an embedding's vertex.
     double edge_biased_degree = 0;
@@ -159,6 +166,8 @@ struct ExpandArgs {
     int32_t nparents;
     int64_t ntiles;
     int32_t in_cols;                   // columns of the parent table
+    int32_t ecol_in = -1;              // first entry column of the parent table, -1 if none
+    int32_t ecol_out = -1;             // first entry column of the child table, -1 if none
     int32_t* const* in_col_ptrs;       // device array [in_cols] of column pointers
     int32_t* const* out_col_ptrs;      // device array [out_cols] (support pass with materialisation)
     LevelKeys keys;
@@ -189,8 +198,9 @@ cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d
                                    int32_t elo, const int32_t* d_elabels_sorted, DevGraph& g, uint64_t* d_tmp,
                                    uint32_t* d_status, cudaStream_t st);
 cudaError_t launch_seed_count(const DevGraph& g, unsigned long long* counts, cudaStream_t st);
+// col2 (may be null) receives each seed's entry index.
 cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* pool, int32_t* col0,
-                                int32_t* col1, uint32_t* status, cudaStream_t st);
+                                int32_t* col1, int32_t* col2, uint32_t* status, cudaStream_t st);
 cudaError_t launch_expand(const ExpandArgs& a, Pass pass, cudaStream_t st);
 cudaError_t launch_domain_sizes(const DomDesc* dom, int32_t nact, const uint32_t* pool,
                                 uint32_t* sizes /* [nact * kMaxV] */, cudaStream_t st);
@@ -204,6 +214,7 @@ struct MaskArgs {
     int32_t nparents;
     int64_t ntiles;
     int32_t* const* in_col_ptrs;
+    int32_t ecol = -1;           // first entry column of the parent table, -1 if none
     unsigned long long* counts;  // level key space
     uint32_t* sizes;             // domain sizes, indexed from ParentMeta::sz_off
     uint32_t* R;                 // zero on entry; the sweep leaves it zero

@@ -68,6 +68,8 @@ void free_graph(gspan_graph* gr, cudaStream_t st)
     if (g.vrank) cudaFreeAsync(g.vrank, st);
     if (g.segmask) cudaFreeAsync(g.segmask, st);
     if (g.selfloop) cudaFreeAsync(g.selfloop, st);
+    if (g.rev) cudaFreeAsync(g.rev, st);
+    g.rev = nullptr;
     if (g.win_base) cudaFreeAsync(g.win_base, st);
     g.win_base = nullptr;
     g.segmask = nullptr;
@@ -312,12 +314,14 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         const size_t words = ((size_t)N + 31) / 32 + 1;
         uint32_t flags = 0;
         UP_CK(cudaMallocAsync(&g.selfloop, words * 4, s), "alloc self-loop bits");
+        if (M > 0) UP_CK(cudaMallocAsync(&g.rev, (size_t)M * 4, s), "alloc reverse entries");
         UP_CK(cudaMemsetAsync(g.selfloop, 0, words * 4, s), "clear self-loop bits");
         UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
         UP_CK(launch_graph_flags(g, ctx->d_status, s), "graph flags launch");
         UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
         UP_CK(cudaStreamSynchronize(s), "graph flags");
         g.symmetric = !(flags & kErrAsymmetric);
+        g.entry_cols = g.symmetric && g.nel == 1;
     }
 #undef UP_CK
     ++ctx->live_graphs;

@@ -346,6 +346,7 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
                                const int32_t* __restrict__ vrank, const int32_t* __restrict__ win_base,
                                int32_t lwin, int32_t nel, LevelKeys keys,
                                uint32_t* __restrict__ pool, int32_t* __restrict__ col0, int32_t* __restrict__ col1,
+                               int32_t* __restrict__ col2,
                                uint32_t* status)
 {
     const int lane = threadIdx.x & 31;
@@ -376,6 +377,7 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
                 const long long row = keys.mat_off[a] + (long long)slot;
                 col0[row] = (int32_t)u;
                 col1[row] = (int32_t)w;
+                if (col2) col2[row] = (int32_t)i;
             } else {
                 atomicOr(status, kErrCursor);
             }
@@ -395,6 +397,7 @@ struct ExpandDev {
     int64_t ntiles;
     int32_t* const* in_cols;
     int32_t* const* out_cols;
+    int32_t ecol_in, ecol_out;   // first entry column of the parent / child table (-1: none)
     LevelKeys keys;
     uint32_t* pool;
     unsigned long long* tile_counter;
@@ -482,6 +485,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
         for (int t = 0; t < nback; ++t) {
             bool ok = false;
             int32_t bel = 0;
+            int32_t bpos = 0;   // entry index of the backward edge found
             if (live) {
                 const int bv = P.back_v[t];
                 const int32_t x = W.img[lane][bv];
@@ -501,6 +505,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                         if (!used) {
                             ok = true;
                             bel = el;
+                            bpos = pos;
                         }
                     }
                 }
@@ -531,6 +536,11 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                     if (slot < a.keys.counts[key]) {
                         const long long r = a.keys.mat_off[ai] + (long long)slot;
                         for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[lane][p];
+                        if (a.ecol_out >= 0) {
+                            for (int j = 0; j < P.nedge; ++j)
+                                a.out_cols[a.ecol_out + j][r] = __ldg(a.in_cols[a.ecol_in + j] + row);
+                            a.out_cols[a.ecol_out + P.nedge][r] = bpos;
+                        }
                     } else {
                         atomicOr(a.status, kErrCursor);   // more candidates than counted: never write past the range
                     }
@@ -544,6 +554,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
             bool ok = item < total;
             int owner = 0;
             uint32_t to = 0;
+            int32_t eidx = 0;   // index of the candidate entry
             int32_t key = 0;
             if (ok) {
                 int l2 = 0, h2 = 31;
@@ -558,7 +569,8 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                     j -= W.cnt[owner][s];
                     ++s;
                 }
-                const uint64_t e = __ldg(a.adj + W.start[owner][s] + j);
+                eidx = W.start[owner][s] + j;
+                const uint64_t e = __ldg(a.adj + eidx);
                 to = entry_to(e);
                 const int32_t tl = (int32_t)entry_tl(e);
                 bool fresh = tl >= min_label && (uint32_t)(tl - P.lbase) < (uint32_t)a.lwin;
@@ -599,6 +611,12 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                         const long long r = a.keys.mat_off[ai] + (long long)slot;
                         for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[owner][p];
                         a.out_cols[nv][r] = (int32_t)to;
+                        if (a.ecol_out >= 0) {
+                            const int64_t orow = P.row_begin + (tile - P.tile_begin) * 32 + owner;
+                            for (int jj = 0; jj < P.nedge; ++jj)
+                                a.out_cols[a.ecol_out + jj][r] = __ldg(a.in_cols[a.ecol_in + jj] + orow);
+                            a.out_cols[a.ecol_out + P.nedge][r] = eidx;
+                        }
                     } else {
                         atomicOr(a.status, kErrCursor);
                     }
@@ -638,6 +656,8 @@ struct MaskDev {
     const uint64_t* adj;
     const uint32_t* segmask;
     const uint32_t* selfloop;
+    const int32_t* rev;
+    int32_t ecol;
     bool symmetric;
     int32_t n, m, nvl, nel, mw, lwin;
     const ParentMeta* parents;
@@ -712,7 +732,7 @@ __global__ void k_segmask(int32_t n, int32_t lwin, int32_t segw, const int32_t* 
 // Thread per entry: self-loop bits, and whether the entry's reverse exists.
 __global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const int32_t* __restrict__ offsets,
                               const uint64_t* __restrict__ adj, const int32_t* __restrict__ vrank,
-                              uint32_t* __restrict__ selfloop, uint32_t* status)
+                              uint32_t* __restrict__ selfloop, int32_t* __restrict__ rev, uint32_t* status)
 {
     bool asym = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
@@ -720,12 +740,19 @@ __global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const 
         const uint32_t u = (uint32_t)src[i], x = entry_to(ent);
         if (u == x) {
             atomicOr(selfloop + (u >> 5), 1u << (u & 31));
+            rev[i] = (int32_t)i;
             continue;
         }
+        // Rank of i among the equal entries before it (parallel edges with one label).
+        int32_t r0 = (int32_t)i;
+        const int32_t bu = offsets[u];
+        while (r0 > bu && adj[r0 - 1] == ent) --r0;
         const uint64_t rk = pack_entry(entry_el(ent), (uint32_t)vrank[u], u);
         const int32_t b = offsets[x], e = offsets[x + 1];
-        const int32_t p = lower_bound_entry(adj, b, e, rk);
-        asym |= p >= e || adj[p] != rk;
+        const int32_t q = lower_bound_entry(adj, b, e, rk) + ((int32_t)i - r0);
+        const bool found = q < e && adj[q] == rk;
+        rev[i] = found ? q : -1;
+        asym |= !found;
     }
     if (__any_sync(kFull, asym) && (threadIdx.x & 31) == 0) atomicOr(status, kErrAsymmetric);
 }
@@ -796,6 +823,77 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
             // H of this source, indexed by batch-wide entry index.
             uint32_t* Hs = a.H + P.h_off + (int64_t)s * P.mloc - P.ebase;
             uint32_t ex[kMaxMaskWords] = {0, 0, 0, 0};
+            if (a.ecol >= 0) {
+                // One edge label.  Images joined to the source by a pattern
+                // edge are found through the row's entry columns (or their
+                // reverse entries); the others by search, after a cheap
+                // existence test from the shorter side.
+                int32_t it_t[kMaxV], it_lb[kMaxV], it_ub[kMaxV];
+                int nit = 0;
+                const int vs = P.src_v[s];
+                for (int j = 0; j < nv; ++j) {
+                    const int t = P.vlab[j];
+                    const uint64_t seg0 = pack_entry(0, (uint32_t)t, 0);
+                    if (t < min_label || seg0 < lo) continue;
+                    const int32_t x = img[j];
+                    bool dup = false;
+                    for (int q = 0; q < j; ++q) dup |= img[q] == x;
+                    if (dup) continue;
+                    const uint64_t key = seg0 | (uint32_t)x;
+                    int jj = -1;
+                    for (int q = 0; q < P.nedge; ++q)
+                        if ((P.e_from[q] == vs && P.e_to[q] == j) || (P.e_to[q] == vs && P.e_from[q] == j)) jj = q;
+                    int32_t pos = -1;
+                    if (jj >= 0) {
+                        const int32_t stored = __ldg(a.in_cols[a.ecol + jj] + row);
+                        pos = P.e_from[jj] == vs ? stored : __ldg(a.rev + stored);
+                        if (pos < b || pos >= e || __ldg(a.adj + pos) != key) pos = -1;   // not where expected: search
+                    }
+                    if (pos < 0) {
+                        if (x == u) {
+                            if (!((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
+                        } else if (jj < 0 && a.symmetric) {
+                            const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
+                            if (4 * (xe - xb) < e - b) {
+                                const uint64_t rk = pack_entry(0, (uint32_t)P.vlab[vs], (uint32_t)u);
+                                const int32_t rp = lower_bound_entry(a.adj, xb, xe, rk);
+                                if (rp >= xe || __ldg(a.adj + rp) != rk) continue;
+                            }
+                        }
+                        pos = lower_bound_entry(a.adj, b, e, key);
+                        if (pos >= e || __ldg(a.adj + pos) != key) continue;
+                    }
+                    int32_t lb = pos, ub = pos + 1;
+                    while (lb > b && __ldg(a.adj + lb - 1) == key) --lb;
+                    while (ub < e && __ldg(a.adj + ub) == key) ++ub;
+                    for (int32_t q = lb; q < ub; ++q) atomicAdd(Hs + q, 1u);
+                    it_t[nit] = t;
+                    it_lb[nit] = lb;
+                    it_ub[nit] = ub;
+                    ++nit;
+                }
+                // A segment is lost to the row when its images fill all of it.
+                for (int i = 0; i < nit; ++i) {
+                    bool lead = true;
+                    for (int q = 0; q < i; ++q) lead &= it_t[q] != it_t[i];
+                    if (!lead) continue;
+                    int32_t hits = 0, minlb = e, maxub = b;
+                    for (int q = i; q < nit; ++q) {
+                        if (it_t[q] != it_t[i]) continue;
+                        hits += it_ub[q] - it_lb[q];
+                        minlb = min(minlb, it_lb[q]);
+                        maxub = max(maxub, it_ub[q]);
+                    }
+                    const uint32_t segk = (uint32_t)(pack_entry(0, (uint32_t)it_t[i], 0) >> 32);
+                    const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
+                    const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
+                    if (first && last && maxub - minlb == hits) {
+                        const uint32_t kc = (uint32_t)(it_t[i] - P.lbase);
+#pragma unroll
+                        for (int w = 0; w < kMaxMaskWords; ++w) ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
+                    }
+                }
+            } else
             for (int el = 0; el < a.nel; ++el) {
                 for (int i = 0; i < nv; ++i) {
                     const int t = P.vlab[i];
@@ -1095,11 +1193,12 @@ cudaError_t launch_seed_count(const DevGraph& g, unsigned long long* counts, cud
 }
 
 cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* pool, int32_t* col0, int32_t* col1,
+                                int32_t* col2,
                                 uint32_t* status, cudaStream_t st)
 {
     if (g.m == 0) return cudaSuccess;
     k_seed_support<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.win_base, g.lwin, g.nel, keys, pool,
-                                                       col0, col1, status);
+                                                       col0, col1, col2, status);
     return cudaGetLastError();
 }
 
@@ -1130,6 +1229,8 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     a.ntiles = x.ntiles;
     a.in_cols = x.in_col_ptrs;
     a.out_cols = x.out_col_ptrs;
+    a.ecol_in = x.ecol_in;
+    a.ecol_out = x.ecol_out;
     a.keys = x.keys;
     a.pool = x.dom_pool;
     a.tile_counter = x.tile_counter;
@@ -1154,7 +1255,8 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
 cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st)
 {
     if (g.m == 0) return cudaSuccess;
-    k_graph_flags<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj, g.vrank, g.selfloop, status);
+    k_graph_flags<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj, g.vrank, g.selfloop, g.rev,
+                                                      status);
     return cudaGetLastError();
 }
 
@@ -1174,6 +1276,8 @@ MaskDev mask_dev(const MaskArgs& x)
     a.adj = x.g->adj;
     a.segmask = x.g->segmask;
     a.selfloop = x.g->selfloop;
+    a.rev = x.g->rev;
+    a.ecol = x.ecol;
     a.symmetric = x.g->symmetric;
     a.n = x.g->n;
     a.m = x.g->m;

@@ -98,6 +98,7 @@ void dfree(T*& p, cudaStream_t st)
 
 struct Table {
     int ncols = 0;
+    int ecol = -1;                // first entry column (one per pattern edge), -1 if none
     int64_t rows = 0;
     std::vector<int32_t*> cols;
     int32_t** d_cols = nullptr;   // device copy of `cols`
@@ -108,6 +109,7 @@ struct Table {
         cols.clear();
         dfree(d_cols, st);
         ncols = 0;
+        ecol = -1;
         rows = 0;
     }
 };
@@ -280,6 +282,11 @@ struct Run {
             GS_CK(cudaMemsetAsync(as.d_cursor, 0, act.size() * 8, s), "clear cursor");
         }
         if (materialize && out_rows > 0) {
+            // One entry column (the seed's entry) follows the vertex columns.
+            if (g.entry_cols) {
+                out.ecol = out_cols;
+                out_cols += 1;
+            }
             out.ncols = out_cols;
             out.rows = out_rows;
             out.cols.assign(out_cols, nullptr);
@@ -362,7 +369,7 @@ struct Run {
         LevelKeys keys{d_counts, as.d_act, as.d_dom, as.d_mat, as.d_cursor};
         if (as.nact > 0) {
             GS_CK(launch_seed_support(g, keys, as.pool, mat ? table.cols[0] : nullptr, mat ? table.cols[1] : nullptr,
-                                      ctx->d_status, s),
+                                      mat && table.ecol >= 0 ? table.cols[table.ecol] : nullptr, ctx->d_status, s),
                   "seed support launch");
             ++st.kernel_launches;
         }
@@ -661,6 +668,7 @@ struct Run {
                 ma.nparents = (int32_t)G.metas.size();
                 ma.ntiles = G.tiles;
                 ma.in_col_ptrs = table.d_cols;
+                ma.ecol = table.ecol;
                 ma.counts = d_counts;
                 ma.sizes = d_sizes;
                 ma.R = d_R;
@@ -690,6 +698,7 @@ struct Run {
         x.g = &g;
         x.in_cols = table.ncols;
         x.in_col_ptrs = table.d_cols;
+        x.ecol_in = table.ecol;
         x.keys.counts = d_counts;
         x.tile_counter = ctx->d_counters;
         x.scanned = ctx->d_counters + 1;
@@ -837,6 +846,11 @@ struct Run {
         GS_CK(copy(d_mat, mat_h.data(), mat_h.size() * sizeof(long long), cudaMemcpyHostToDevice, s), "copy mat");
         GS_CK(dalloc(&d_cur, freq.size(), s), "alloc cursor");
         GS_CK(cudaMemsetAsync(d_cur, 0, freq.size() * 8, s), "clear cursor");
+        // Entry columns (one per pattern edge of the children) follow.
+        if (table.ecol >= 0) {
+            out.ecol = ncols;
+            ncols += size + 1;
+        }
         out.ncols = ncols;
         out.rows = rows;
         out.cols.assign(ncols, nullptr);
@@ -877,6 +891,7 @@ struct Run {
         x.ntiles = atiles;
         x.keys = LevelKeys{d_counts, d_act, nullptr, d_mat, d_cur};
         x.out_col_ptrs = out.d_cols;
+        x.ecol_out = out.ecol;
         tic(&e0, &e1);
         GS_CK(launch_expand(x, Pass::Materialize, s), "materialise launch");
         toc(e0, e1, &st.materialize_ms);
