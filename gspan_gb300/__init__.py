@@ -111,6 +111,25 @@ _lib.gspan_mine_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int
 _lib.gspan_mine_batch.restype = ctypes.c_int
 _lib.gspan_graph_instances.argtypes = [ctypes.c_void_p]
 _lib.gspan_graph_instances.restype = ctypes.c_int32
+class JobInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("queued_ms", ctypes.c_double), ("run_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double), ("predicted_bytes", ctypes.c_double),
+                ("retried_alone", ctypes.c_int32), ("stats", Stats)]
+
+
+_lib.gspan_server_create.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]
+_lib.gspan_server_create.restype = ctypes.c_int
+_lib.gspan_server_destroy.argtypes = [ctypes.c_void_p]
+_lib.gspan_server_destroy.restype = None
+_lib.gspan_server_add_graph.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
+_lib.gspan_server_add_graph.restype = ctypes.c_int
+_lib.gspan_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.POINTER(ctypes.c_int64)]
+_lib.gspan_server_submit.restype = ctypes.c_int
+_lib.gspan_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_int64, EMIT_FN, ctypes.c_void_p,
+                                   ctypes.POINTER(JobInfo)]
+_lib.gspan_server_wait.restype = ctypes.c_int
 _lib.gspan_table_support.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]
 _lib.gspan_table_support.restype = ctypes.c_int
@@ -130,7 +149,8 @@ _lib.gspan_max_pattern_edges.restype = ctypes.c_int32
 ABI_SYMBOLS = ("gspan_opts_default", "gspan_ctx_create", "gspan_ctx_destroy", "gspan_graph_upload",
                "gspan_graph_free", "gspan_mine", "gspan_batch_upload", "gspan_mine_batch", "gspan_graph_instances",
                "gspan_table_support", "gspan_table_support_noalloc",
-               "gspan_is_canonical",
+               "gspan_server_create", "gspan_server_destroy", "gspan_server_add_graph", "gspan_server_submit",
+               "gspan_server_wait", "gspan_is_canonical",
                "gspan_status_string", "gspan_last_error", "gspan_max_pattern_edges")
 
 Code = tuple  # tuple of (from, to, from_label, edge_label, to_label)
@@ -297,6 +317,70 @@ class Miner:
         if self._ctx:
             _lib.gspan_ctx_destroy(self._ctx)
             self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop (gspan_server_*): resident graphs, jobs queued as they
+    arrive, run on `slots` concurrent contexts with byte-budget admission."""
+
+    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 0.0):
+        self._s = ctypes.c_void_p()
+        rc = _lib.gspan_server_create(device, slots, float(budget_bytes), ctypes.byref(self._s))
+        if rc != GSPAN_OK:
+            raise GspanError(rc, "gspan_server_create")
+
+    def add_graph(self, g: CSR) -> int:
+        off = np.ascontiguousarray(g.offsets, dtype=np.int32)
+        vl = np.ascontiguousarray(g.vlabels, dtype=np.int32)
+        ed = np.ascontiguousarray(g.edges, dtype=np.int32).reshape(-1, 3)
+        gid = ctypes.c_int32()
+        rc = _lib.gspan_server_add_graph(self._s, g.n, g.m, off.ctypes.data, vl.ctypes.data if g.n else None,
+                                         ed.ctypes.data if g.m else None, ctypes.byref(gid))
+        if rc != GSPAN_OK:
+            raise GspanError(rc, "gspan_server_add_graph")
+        return gid.value
+
+    def submit(self, graph_id: int, k: int, min_support: int) -> int:
+        jid = ctypes.c_int64()
+        rc = _lib.gspan_server_submit(self._s, graph_id, int(k), int(min_support), ctypes.byref(jid))
+        if rc != GSPAN_OK:
+            raise GspanError(rc, "gspan_server_submit")
+        return jid.value
+
+    def wait(self, job_id: int):
+        """Returns (patterns, info dict) of a finished job (blocks until done)."""
+        out: list = []
+
+        def emit(_user, code, length, support):
+            out.append((tuple((code[i].frm, code[i].to, code[i].from_label, code[i].edge_label,
+                               code[i].to_label) for i in range(length)), int(support)))
+            return 0
+
+        cb = EMIT_FN(emit)
+        info = JobInfo()
+        rc = _lib.gspan_server_wait(self._s, int(job_id), cb, None, ctypes.byref(info))
+        if rc != GSPAN_OK:
+            raise GspanError(rc, "gspan_server_wait")
+        d = {name: getattr(info, name) for name, _ in info._fields_ if name != "stats"}
+        d["stats"] = info.stats.as_dict()
+        return out, d
+
+    def close(self) -> None:
+        if self._s:
+            _lib.gspan_server_destroy(self._s)
+            self._s = ctypes.c_void_p()
 
     def __enter__(self):
         return self

@@ -152,7 +152,8 @@ gspan_status gspan_mine(gspan_ctx* ctx, const gspan_graph* graph, int32_t k, int
                         gspan_emit_fn emit, void* user, gspan_stats* stats)
 {
     if (!ctx || !graph) return GSPAN_ERR_INVALID;
-    if (graph->owner != ctx) return fail(ctx, GSPAN_ERR_INVALID, "graph belongs to another context");
+    if (graph->owner->device != ctx->device)
+        return fail(ctx, GSPAN_ERR_INVALID, "graph was uploaded to another device");
     ctx->err.clear();
     if (graph->g.ninst != 1) return fail(ctx, GSPAN_ERR_INVALID, "a batch is mined with gspan_mine_batch");
     cudaError_t e = cudaSetDevice(ctx->device);
@@ -176,7 +177,8 @@ gspan_status gspan_mine_batch(gspan_ctx* ctx, const gspan_graph* batch, int32_t 
                               gspan_batch_emit_fn emit, void* user, gspan_stats* stats)
 {
     if (!ctx || !batch || !min_support) return GSPAN_ERR_INVALID;
-    if (batch->owner != ctx) return fail(ctx, GSPAN_ERR_INVALID, "graph belongs to another context");
+    if (batch->owner->device != ctx->device)
+        return fail(ctx, GSPAN_ERR_INVALID, "graph was uploaded to another device");
     ctx->err.clear();
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "set device");

@@ -546,7 +546,9 @@ struct Run {
         double rows_bytes = 0, cand_read_bytes = 0, all_read_bytes = 0;
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
-        const double budget = std::max(2.0e9, 0.4 * (double)free_b);
+        // The mask groups may hold this share of the free device memory.
+        const double share = ctx->opts.mem_fraction > 0 ? std::min(0.4, ctx->opts.mem_fraction) : 0.4;
+        const double budget = std::max(2.5e8, share * (double)free_b);
         for (int i = 0; i < np; ++i) {
             ParentMeta& A = all[i];
             const int64_t rows = A.row_end - A.row_begin;

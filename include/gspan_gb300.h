@@ -15,8 +15,10 @@
  *   gspan_is_canonical  <- is_canonical(const DFSCode&)     (gspan.cu:586-606)
  *
  * Threading: a context is used by one host thread at a time.  A context owns
- * its CUDA stream and all device memory it allocates; graphs are owned by the
- * context that uploaded them and must be freed before it is destroyed.
+ * its CUDA stream and all device memory it allocates.  A graph is freed by
+ * the context that uploaded it (before that context is destroyed) and may be
+ * mined by any context on the same device, from any number of threads at
+ * once: mining only reads it.
  */
 #ifndef GSPAN_GB300_H_
 #define GSPAN_GB300_H_
@@ -55,7 +57,8 @@ typedef struct gspan_opts {
     int32_t domain_mode;         /* 0 auto (bitmap or hashset per domain), 1 bitmaps only, 2 hashsets only */
     double hash_threshold;       /* auto mode: a domain uses a hashset when 64 * max_size < |V| * hash_threshold.
                                     0 selects the default (1.0) */
-    double mem_fraction;         /* share of free device memory the miner may hold (0 = 0.85) */
+    double mem_fraction;         /* share of free device memory one level's mask-path arrays may hold
+                                    (capped at 0.4; 0 selects 0.4) */
     int32_t profile;             /* 1: time every kernel launch with CUDA events into gspan_stats */
     int32_t path;                /* extension kernels: 0 auto, 1 per-candidate only, 2 mask path wherever the
                                     label space allows (both give identical results) */
@@ -149,6 +152,41 @@ gspan_status gspan_mine_batch(gspan_ctx* ctx, const gspan_graph* batch, int32_t 
 
 /* Number of instances in an uploaded graph (1 for gspan_graph_upload). */
 int32_t gspan_graph_instances(const gspan_graph* graph);
+
+/* ---- Serving: requests accepted as they arrive, overlapping on the GPU ----
+ * No counterpart in the reference (one graph per process run).  Graphs are
+ * uploaded once and stay resident.  `slots` worker threads, each with its
+ * own context and stream, run admitted jobs concurrently; a job is exactly a
+ * gspan_mine call, so its result is the same alone or in a mix.  Admission is
+ * first come, first served: the oldest waiting job starts when a slot is free
+ * and its predicted working bytes fit `budget_bytes` (0: 60 % of the free
+ * device memory) beside the running jobs; a job that runs out of device
+ * memory beside others is re-run alone.  A server is driven by one host
+ * thread (submit/wait); the workers are internal. */
+typedef struct gspan_server gspan_server;
+
+typedef struct gspan_job_info {
+    gspan_status status;
+    double queued_ms;            /* submit -> start */
+    double run_ms;               /* start -> done */
+    double latency_ms;           /* submit -> done */
+    double predicted_bytes;      /* admission estimate */
+    int32_t retried_alone;       /* 1: ran out of memory beside others and was re-run alone */
+    gspan_stats stats;
+} gspan_job_info;
+
+gspan_status gspan_server_create(int32_t device, int32_t slots, double budget_bytes, gspan_server** out);
+/* Waits for the running jobs, then frees the graphs, contexts and server. */
+void gspan_server_destroy(gspan_server* server);
+gspan_status gspan_server_add_graph(gspan_server* server, int32_t nr_nodes, int32_t nr_edges, const int32_t* offsets,
+                                    const int32_t* vlabels, const gspan_edge* edges, int32_t* graph_id);
+/* Queues a job; returns at once with its id. */
+gspan_status gspan_server_submit(gspan_server* server, int32_t graph_id, int32_t k, int32_t min_support,
+                                 int64_t* job_id);
+/* Blocks until the job is done, emits its patterns (pre-order) and fills
+ * `info` (may be NULL); returns the job's status.  Each id is waited once. */
+gspan_status gspan_server_wait(gspan_server* server, int64_t job_id, gspan_emit_fn emit, void* user,
+                               gspan_job_info* info);
 
 /* MNI support of an embedding table in device memory (the reference's
  * support_gpu, gspan.cu:200-289, for a column table): `cols` is a host array
