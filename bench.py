@@ -20,6 +20,11 @@ cpu_baseline = the CPU oracle port (the reference's algorithm, OpenMP on all
          host cores) on a bounded sample of the same workload: the same graph
          and threshold at 2 edges.
 
+--workload serving: a Poisson stream (mean --rate jobs/s) of jobs over
+resident graphs of the three single-graph sizes; jobs/s with p50/p95/p99
+latency, each result checked against the same job run alone.
+--workload batch_256: the batched engine against the plain one.
+
 --impl reference times that CPU implementation alone (rank 0; other ranks
 exit) and prints the same line with "impl": "reference".
 
@@ -373,6 +378,96 @@ def batch_arm(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def serving_arm(args) -> None:
+    """Serving: a Poisson stream (mean 50 jobs/s) of mining jobs over a
+    resident pool of graphs of the three single-graph sizes (70/25/5 %), min
+    support uniform in [1 %, 5 %] of n.  A step is one stream of
+    --serving-jobs jobs submitted at their arrival times to a server with
+    --slots concurrent contexts; every job's result is checked against the
+    same job run alone (a one-slot server, before the timed steps)."""
+    import threading
+    import torch
+    from gspan_gb300 import Server, datagen
+    t0 = time.time()
+    pool = datagen.serving_pool(4)
+    gen_s = time.time() - t0
+    classes = [c for c, _ in pool]
+    sizes = [g.n for _, g in pool]
+
+    def run_stream(srv, ids, jobs):
+        handles = [None] * len(jobs)
+        start = time.perf_counter()
+
+        def submit():
+            for j, (t, gi, k, sup) in enumerate(jobs):
+                delay = start + t - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                handles[j] = srv.submit(ids[gi], k, sup)
+
+        th = threading.Thread(target=submit)
+        th.start()
+        out = []
+        for j in range(len(jobs)):
+            while handles[j] is None:
+                time.sleep(0.0005)
+            out.append(srv.wait(handles[j]))
+        th.join()
+        return out, time.perf_counter() - start
+
+    results = []
+    with Server(slots=1) as alone_srv:
+        ids = [alone_srv.add_graph(g) for _, g in pool]
+        rate = args.rate if args.rate > 0 else 50.0
+        stream_jobs = [datagen.serving_jobs(classes, sizes, args.serving_jobs, rate, seed=40 + i)
+                       for i in range(args.steps)]
+        if args.rate <= 0:   # capacity: every job of a stream arrives at once
+            stream_jobs = [[(0.0,) + j[1:] for j in jobs] for jobs in stream_jobs]
+        alone = []
+        for jobs in stream_jobs:
+            alone.append([alone_srv.wait(alone_srv.submit(ids[gi], k, sup))[0] for _, gi, k, sup in jobs])
+    torch.cuda.synchronize()
+    with Server(slots=args.slots) as srv:
+        ids = [srv.add_graph(g) for _, g in pool]
+        warm = [(0.0 if args.rate <= 0 else t, gi, k, sup)
+                for t, gi, k, sup in datagen.serving_jobs(classes, sizes, args.serving_jobs, rate, seed=30)]
+        for _ in range(args.warmup):
+            run_stream(srv, ids, warm)
+        lat, qms, ext, walls, retried = [], [], 0, [], 0
+        with ClockSampler(0) as clk:
+            for step, jobs in enumerate(stream_jobs):
+                out, wall = run_stream(srv, ids, jobs)
+                walls.append(wall)
+                for j, (res, info) in enumerate(out):
+                    assert res == alone[step][j], f"job {j} of stream {step} differs from its result alone"
+                    lat.append(info["latency_ms"])
+                    qms.append(info["queued_ms"])
+                    ext += info["stats"]["extended"]
+                    retried += info["retried_alone"]
+        clocks = clk.summary()
+    lat.sort()
+
+    def pct(p):
+        return lat[min(len(lat) - 1, int(round(p / 100.0 * (len(lat) - 1))))]
+
+    njobs = len(lat)
+    line = {
+        "metric": "serving: jobs/s with p50/p95/p99 job latency (exact patterns+MNI)", "value": njobs / sum(walls),
+        "unit": "jobs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.median(walls), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "config": {"workload": "serving", "rate_jobs_per_s": args.rate if args.rate > 0 else "all at once", "jobs_per_step": args.serving_jobs,
+                   "slots": args.slots, "mix": "70/25/5 % Erdos-Renyi 3,300 V / Chung-Lu 100,000 V / "
+                   "Chung-Lu 3,700,000 V (8/3/1 resident graphs, seed 4)",
+                   "min_support": "uniform [1 %, 5 %] of n", "k": "3 or 4 (3,300 V), 3 (others)"},
+        "latency_ms": {"p50": pct(50), "p95": pct(95), "p99": pct(99), "max": lat[-1],
+                       "mean_queued": statistics.mean(qms)},
+        "embeddings_per_s": ext / sum(walls), "jobs": njobs, "retried_alone": retried,
+        "all_equal_alone": True, "generate_s": gen_s, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -381,7 +476,13 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", default="chung_lu_100k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--slots", type=int, default=4, help="serving: concurrent contexts")
+    ap.add_argument("--serving-jobs", type=int, default=100, help="serving: jobs per stream (one step)")
+    ap.add_argument("--rate", type=float, default=50.0, help="serving: mean arrivals per second (0: all at once)")
     args = ap.parse_args()
+    if args.workload == "serving":
+        serving_arm(args)
+        return
     if args.workload in ("batch_256", "batch_16"):
         batch_arm(args)
         return

@@ -38,6 +38,8 @@ if not os.path.exists(LIB_PATH):
 _lib = ctypes.CDLL(LIB_PATH)
 
 GSPAN_OK = 0
+GSPAN_ERR_INVALID = 1
+GSPAN_ERR_NOMEM = 3
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "LIMIT", 5: "DEVICE", 6: "ABORTED",
                 7: "NO_DEVICE"}
 

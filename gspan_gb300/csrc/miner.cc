@@ -31,6 +31,7 @@
 #include <functional>
 #include <limits>
 #include <tuple>
+#include <unordered_set>
 
 namespace gs {
 
@@ -43,6 +44,10 @@ gspan_status fail(gspan_ctx* ctx, gspan_status s, const std::string& msg)
 gspan_status cuda_fail(gspan_ctx* ctx, cudaError_t e, const char* what)
 {
     const gspan_status s = (e == cudaErrorMemoryAllocation) ? GSPAN_ERR_NOMEM : GSPAN_ERR_CUDA;
+    // Running out of memory leaves the context usable, but the runtime keeps
+    // the error as this thread's last error, where the next launch check
+    // would find it again.
+    if (e == cudaErrorMemoryAllocation) cudaGetLastError();
     return fail(ctx, s, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
@@ -81,20 +86,41 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Device blocks held by the mining run on this thread.  Whatever an early
+// error return leaves behind is freed when the run ends (LiveBlocks).
+thread_local std::unordered_set<void*>* t_live = nullptr;
+
 template <class T>
 cudaError_t dalloc(T** p, size_t count, cudaStream_t st)
 {
     *p = nullptr;
     if (count == 0) return cudaSuccess;
-    return cudaMallocAsync(reinterpret_cast<void**>(p), count * sizeof(T), st);
+    const cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(p), count * sizeof(T), st);
+    if (e != cudaSuccess) *p = nullptr;
+    else if (t_live) t_live->insert(*p);
+    return e;
 }
 
 template <class T>
 void dfree(T*& p, cudaStream_t st)
 {
-    if (p) cudaFreeAsync(p, st);
+    if (p) {
+        if (t_live) t_live->erase(p);
+        cudaFreeAsync(p, st);
+    }
     p = nullptr;
 }
+
+struct LiveBlocks {
+    std::unordered_set<void*> blocks;
+    cudaStream_t s;
+    explicit LiveBlocks(cudaStream_t st) : s(st) { t_live = &blocks; }
+    ~LiveBlocks()
+    {
+        for (void* p : blocks) cudaFreeAsync(p, s);
+        t_live = nullptr;
+    }
+};
 
 struct Table {
     int ncols = 0;
@@ -930,6 +956,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<in
     // set-up); here it is an argument error.
     if (k < 1) return fail(ctx, GSPAN_ERR_INVALID, "k must be at least 1");
     if (k > kMaxE) return fail(ctx, GSPAN_ERR_LIMIT, "k exceeds the largest supported pattern size");
+    LiveBlocks live(ctx->stream);
     Run run{ctx, g, k, minsup};
     run.s = ctx->stream;
     run.profile = ctx->opts.profile != 0;

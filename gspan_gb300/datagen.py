@@ -273,3 +273,45 @@ def batch_instances(seed: int = 2, count: int = 256) -> tuple[list[CSR], list[in
         graphs.append(chung_lu(n, m, 2.1, nlabels, 1.0, seed * 1000003 + i, max_deg=math.sqrt(2.0 * m)))
         sups.append(int(0.02 * n))
     return graphs, sups
+
+
+# Serving: a resident pool of graphs of the three single-graph sizes, and a
+# Poisson stream of jobs drawn over it.
+SERVING_CLASSES = ("er_3300", "chung_lu_100k", "chung_lu_3_7m")
+SERVING_MIX = (0.70, 0.25, 0.05)
+
+
+def serving_pool(seed: int = 4, per_class: tuple[int, int, int] = (8, 3, 1)) -> list[tuple[int, CSR]]:
+    """(size class, graph) pairs with fresh seeds: per_class[c] graphs of
+    class c (Erdos-Renyi 3,300 V; Chung-Lu 100,000 V; Chung-Lu 3,700,000 V)."""
+    makers = (er_3300, chung_lu_100k, chung_lu_3_7m)
+    pool = []
+    for c, (make, cnt) in enumerate(zip(makers, per_class)):
+        for i in range(cnt):
+            pool.append((c, make(seed * 1000 + 100 * c + i)))
+    return pool
+
+
+def serving_jobs(pool_classes: list[int], pool_sizes: list[int], count: int, rate: float = 50.0,
+                 seed: int = 4) -> list[tuple[float, int, int, int]]:
+    """`count` jobs (arrival seconds, pool index, k, min support): exponential
+    inter-arrival times of mean 1/rate, size class drawn by SERVING_MIX, a
+    graph of that class uniformly, min support uniform in [1 %, 5 %] of its
+    vertex count.  k is 3 or 4 (even odds) for the 3,300-vertex class and 3
+    for the others, whose four-edge levels need a level-3 embedding table
+    larger than the device at these supports."""
+    u = rand_unit(seed, 31, 0, count * 5).reshape(count, 5)
+    by_class = [[i for i, c in enumerate(pool_classes) if c == cls] for cls in range(len(SERVING_MIX))]
+    cum = np.cumsum(SERVING_MIX)
+    t = 0.0
+    jobs = []
+    for j in range(count):
+        t += -math.log(1.0 - u[j, 0]) / rate
+        cls = int(np.searchsorted(cum, u[j, 1] * cum[-1], side="right"))
+        cls = min(cls, len(SERVING_MIX) - 1)
+        members = by_class[cls]
+        gi = members[min(len(members) - 1, int(u[j, 2] * len(members)))]
+        k = (3 if u[j, 3] < 0.5 else 4) if cls == 0 else 3
+        sup = max(1, int(pool_sizes[gi] * (0.01 + 0.04 * u[j, 4])))
+        jobs.append((t, gi, k, sup))
+    return jobs
