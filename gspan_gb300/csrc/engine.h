@@ -34,6 +34,7 @@ enum : uint32_t {
     kErrBadGraph = 1u << 1,     // upload validation: offsets or entries inconsistent
     kErrCursor = 1u << 2,       // a materialisation cursor ran past its reserved rows
     kErrAsymmetric = 1u << 3,   // upload: an entry without its reverse entry (not an error)
+    kFlagParallel = 1u << 4,    // upload: two equal entries of one vertex (parallel edges; not an error)
 };
 
 // The graph in HBM.  Labels are replaced by their rank among the distinct
@@ -73,6 +74,15 @@ struct DevGraph {
     // most adjacency searches of the mask row pass.
     int32_t* rev = nullptr;
     bool entry_cols = false;
+    // Edge index: open addressing over `eidx_cap` (a power of two) 64-bit
+    // slots, one per run of equal entries, keyed by (vertex, edge label, to):
+    // slot = fingerprint << 32 | index of the run's first entry, empty = ~0.
+    // An edge lookup is one or two L2 probes instead of a binary search over
+    // the adjacency.  Not built (null) above 2^30 entries.
+    uint64_t* eidx = nullptr;
+    uint32_t eidx_cap = 0;
+    // Some vertex has two equal entries (parallel edges with one label).
+    bool parallel = true;
     // Mean degree of a vertex reached through an edge (sum d^2 / sum d): the
     // expected adjacency length behind an embedding's vertex.
     double edge_biased_degree = 0;
@@ -234,6 +244,9 @@ cudaError_t launch_segmask(DevGraph& g, cudaStream_t st);
 // Self-loop bitmap (zeroed by the caller) and the symmetry check: sets
 // kErrAsymmetric in *status when some entry has no reverse entry.
 cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st);
+// Fills g.eidx (all slots ~0 on entry); sets kFlagParallel in *status when a
+// vertex has two equal entries, kErrHashFull if a probe ran through the table.
+cudaError_t launch_edge_index(DevGraph& g, uint32_t* status, cudaStream_t st);
 cudaError_t launch_mask_rows(const MaskArgs& a, cudaStream_t st);
 // Prefix of the touched lists, then the sweep (two launches).
 cudaError_t launch_mask_sweep(const MaskArgs& a, cudaStream_t st);

@@ -70,6 +70,9 @@ void free_graph(gspan_graph* gr, cudaStream_t st)
     if (g.selfloop) cudaFreeAsync(g.selfloop, st);
     if (g.rev) cudaFreeAsync(g.rev, st);
     g.rev = nullptr;
+    if (g.eidx) cudaFreeAsync(g.eidx, st);
+    g.eidx = nullptr;
+    g.eidx_cap = 0;
     if (g.win_base) cudaFreeAsync(g.win_base, st);
     g.win_base = nullptr;
     g.segmask = nullptr;
@@ -322,6 +325,25 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         UP_CK(cudaStreamSynchronize(s), "graph flags");
         g.symmetric = !(flags & kErrAsymmetric);
         g.entry_cols = g.symmetric && g.nel == 1;
+    }
+    // Edge index at a load factor in (3/8, 3/4].
+    g.parallel = true;
+    if (M > 0 && M <= (1 << 30)) {
+        uint32_t cap = 64;
+        while ((uint64_t)cap < (uint64_t)M + M / 3) cap <<= 1;
+        uint32_t flags = 0;
+        UP_CK(cudaMallocAsync(&g.eidx, (size_t)cap * 8, s), "alloc edge index");
+        g.eidx_cap = cap;
+        UP_CK(cudaMemsetAsync(g.eidx, 0xFF, (size_t)cap * 8, s), "clear edge index");
+        UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
+        UP_CK(launch_edge_index(g, ctx->d_status, s), "edge index launch");
+        UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
+        UP_CK(cudaStreamSynchronize(s), "edge index");
+        if (flags & kErrHashFull) {
+            drop();
+            return fail(ctx, GSPAN_ERR_CUDA, "edge index: a probe ran through the table");
+        }
+        g.parallel = (flags & kFlagParallel) != 0;
     }
 #undef UP_CK
     ++ctx->live_graphs;

@@ -92,6 +92,42 @@ __device__ __forceinline__ int32_t lower_bound_entry(const uint64_t* __restrict_
     return b;
 }
 
+// Edge index hash of (vertex, edge label, to): the 64-bit finaliser of
+// MurmurHash3 over the packed triple.  Low bits pick the slot, high 32 bits
+// are the slot's fingerprint.
+__device__ __forceinline__ uint64_t edge_hash(uint32_t u, uint32_t el, uint32_t to)
+{
+    uint64_t h = (((uint64_t)u << 32) | to) + (uint64_t)(el + 1) * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 33;
+    h *= 0xff51afd7ed558ccdull;
+    h ^= h >> 33;
+    h *= 0xc4ceb9fe1a85ec53ull;
+    h ^= h >> 33;
+    return h;
+}
+
+// First index of `key` (packed edge label, to label, to) in u's adjacency
+// adj[b, e), or -1: probes the edge index from the key's slot to the first
+// empty slot.  A slot is taken only when its entry lies in [b, e) and holds
+// `key`, so fingerprint collisions cannot give a wrong answer.
+__device__ __forceinline__ int32_t edge_find(const uint64_t* __restrict__ eidx, uint32_t cap,
+                                             const uint64_t* __restrict__ adj, int32_t b, int32_t e, uint32_t u,
+                                             uint64_t key)
+{
+    const uint64_t h = edge_hash(u, entry_el(key), entry_to(key));
+    const uint32_t fp = (uint32_t)(h >> 32);
+    uint32_t i = (uint32_t)h & (cap - 1);
+    for (uint32_t probe = 0; probe < cap; ++probe) {
+        const uint64_t slot = __ldg(eidx + i);
+        const uint32_t pos = (uint32_t)slot;
+        if (pos == 0xFFFFFFFFu) return -1;
+        if ((uint32_t)(slot >> 32) == fp && (int32_t)pos >= b && (int32_t)pos < e && __ldg(adj + pos) == key)
+            return (int32_t)pos;
+        i = (i + 1) & (cap - 1);
+    }
+    return -1;
+}
+
 // ---------------------------------------------------------------------------
 // Graph store build.
 
@@ -391,6 +427,8 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
 struct ExpandDev {
     const int32_t* offsets;
     const uint64_t* adj;
+    const uint64_t* eidx;        // edge index (null: binary search)
+    uint32_t eidx_cap;
     int32_t nvl, nel, lwin;
     const ParentMeta* parents;
     int32_t nparents;
@@ -494,8 +532,14 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                 const int32_t b = __ldg(a.offsets + un), e = __ldg(a.offsets + un + 1);
                 for (int32_t el = P.back_eq[t] ? P.back_el[t] : P.back_el[t] + 1; el < a.nel && !ok; ++el) {
                     const uint64_t want = pack_entry((uint32_t)el, tlx, (uint32_t)x);
-                    const int32_t pos = lower_bound_entry(a.adj, b, e, want);
-                    if (pos < e && __ldg(a.adj + pos) == want) {
+                    int32_t pos;
+                    if (a.eidx) {
+                        pos = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)un, want);
+                    } else {
+                        pos = lower_bound_entry(a.adj, b, e, want);
+                        if (pos >= e || __ldg(a.adj + pos) != want) pos = -1;
+                    }
+                    if (pos >= 0) {
                         bool used = false;
                         for (int j = 0; j < P.nedge; ++j) {
                             if (P.e_el[j] != el) continue;
@@ -657,8 +701,11 @@ struct MaskDev {
     const uint32_t* segmask;
     const uint32_t* selfloop;
     const int32_t* rev;
+    const uint64_t* eidx;        // edge index (null: binary search)
+    uint32_t eidx_cap;
     int32_t ecol;
     bool symmetric;
+    bool parallel;               // equal entries may follow each other
     int32_t n, m, nvl, nel, mw, lwin;
     const ParentMeta* parents;
     int32_t nparents;
@@ -757,6 +804,34 @@ __global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const 
     if (__any_sync(kFull, asym) && (threadIdx.x & 31) == 0) atomicOr(status, kErrAsymmetric);
 }
 
+// Thread per entry: the first entry of each run of equal entries goes into
+// the edge index (linear probing, bounded by the table size).
+__global__ void k_edge_index(int32_t m, const int32_t* __restrict__ src, const int32_t* __restrict__ offsets,
+                             const uint64_t* __restrict__ adj, unsigned long long* __restrict__ eidx, uint32_t cap,
+                             uint32_t* status)
+{
+    bool parallel = false, full = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t ent = adj[i];
+        const int32_t u = src[i];
+        if (i > offsets[u] && adj[i - 1] == ent) {
+            parallel = true;
+            continue;
+        }
+        const uint64_t h = edge_hash((uint32_t)u, entry_el(ent), entry_to(ent));
+        const unsigned long long val = ((h >> 32) << 32) | (uint32_t)i;
+        uint32_t j = (uint32_t)h & (cap - 1);
+        uint32_t probe = 0;
+        for (; probe < cap; ++probe) {
+            if (atomicCAS(eidx + j, ~0ull, val) == ~0ull) break;
+            j = (j + 1) & (cap - 1);
+        }
+        full |= probe == cap;
+    }
+    const unsigned pm = __ballot_sync(kFull, parallel), fm = __ballot_sync(kFull, full);
+    if ((threadIdx.x & 31) == 0 && (pm | fm)) atomicOr(status, (pm ? kFlagParallel : 0u) | (fm ? kErrHashFull : 0u));
+}
+
 __device__ __forceinline__ int32_t find_parent_tile(const ParentMeta* parents, int32_t np, long long tile)
 {
     int32_t lo = 0, hi = np - 1;
@@ -850,22 +925,28 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                         if (pos < b || pos >= e || __ldg(a.adj + pos) != key) pos = -1;   // not where expected: search
                     }
                     if (pos < 0) {
-                        if (x == u) {
-                            if (!((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
-                        } else if (jj < 0 && a.symmetric) {
-                            const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
-                            if (4 * (xe - xb) < e - b) {
-                                const uint64_t rk = pack_entry(0, (uint32_t)P.vlab[vs], (uint32_t)u);
-                                const int32_t rp = lower_bound_entry(a.adj, xb, xe, rk);
-                                if (rp >= xe || __ldg(a.adj + rp) != rk) continue;
+                        if (x == u && !((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
+                        if (a.eidx) {
+                            pos = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)u, key);
+                            if (pos < 0) continue;
+                        } else {
+                            if (x != u && jj < 0 && a.symmetric) {
+                                const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
+                                if (4 * (xe - xb) < e - b) {
+                                    const uint64_t rk = pack_entry(0, (uint32_t)P.vlab[vs], (uint32_t)u);
+                                    const int32_t rp = lower_bound_entry(a.adj, xb, xe, rk);
+                                    if (rp >= xe || __ldg(a.adj + rp) != rk) continue;
+                                }
                             }
+                            pos = lower_bound_entry(a.adj, b, e, key);
+                            if (pos >= e || __ldg(a.adj + pos) != key) continue;
                         }
-                        pos = lower_bound_entry(a.adj, b, e, key);
-                        if (pos >= e || __ldg(a.adj + pos) != key) continue;
                     }
                     int32_t lb = pos, ub = pos + 1;
-                    while (lb > b && __ldg(a.adj + lb - 1) == key) --lb;
-                    while (ub < e && __ldg(a.adj + ub) == key) ++ub;
+                    if (a.parallel) {
+                        while (lb > b && __ldg(a.adj + lb - 1) == key) --lb;
+                        while (ub < e && __ldg(a.adj + ub) == key) ++ub;
+                    }
                     for (int32_t q = lb; q < ub; ++q) atomicAdd(Hs + q, 1u);
                     it_t[nit] = t;
                     it_lb[nit] = lb;
@@ -915,7 +996,7 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                         // shorter side when the graph is symmetric.
                         if (x == u) {
                             if (!((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
-                        } else if (a.symmetric && !((P.src_adj[s] >> j) & 1)) {
+                        } else if (!a.eidx && a.symmetric && !((P.src_adj[s] >> j) & 1)) {
                             const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
                             if (4 * (xe - xb) < e - b) {
                                 const uint64_t rk = pack_entry((uint32_t)el, (uint32_t)P.vlab[P.src_v[s]], (uint32_t)u);
@@ -924,7 +1005,13 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                             }
                         }
                         const uint64_t key = seg0 | (uint32_t)x;
-                        const int32_t lb = lower_bound_entry(a.adj, b, e, key);
+                        int32_t lb;
+                        if (a.eidx) {
+                            lb = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)u, key);
+                            if (lb < 0) continue;
+                        } else {
+                            lb = lower_bound_entry(a.adj, b, e, key);
+                        }
                         int32_t ub = lb;
                         while (ub < e && __ldg(a.adj + ub) == key) {
                             atomicAdd(Hs + ub, 1u);
@@ -972,8 +1059,14 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                 const int32_t b = __ldg(a.offsets + un), e = __ldg(a.offsets + un + 1);
                 for (int32_t el = P.back_eq[t] ? P.back_el[t] : P.back_el[t] + 1; el < a.nel && !ok; ++el) {
                     const uint64_t want = pack_entry((uint32_t)el, tlx, (uint32_t)x);
-                    const int32_t pos = lower_bound_entry(a.adj, b, e, want);
-                    if (pos < e && __ldg(a.adj + pos) == want) {
+                    int32_t pos;
+                    if (a.eidx) {
+                        pos = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)un, want);
+                    } else {
+                        pos = lower_bound_entry(a.adj, b, e, want);
+                        if (pos >= e || __ldg(a.adj + pos) != want) pos = -1;
+                    }
+                    if (pos >= 0) {
                         bool used = false;
                         for (int j = 0; j < P.nedge; ++j) {
                             if (P.e_el[j] != el) continue;
@@ -1221,6 +1314,8 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     ExpandDev a;
     a.offsets = x.g->offsets;
     a.adj = x.g->adj;
+    a.eidx = x.g->eidx;
+    a.eidx_cap = x.g->eidx_cap;
     a.nvl = x.g->nvl;
     a.nel = x.g->nel;
     a.lwin = x.g->lwin;
@@ -1260,6 +1355,14 @@ cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st)
     return cudaGetLastError();
 }
 
+cudaError_t launch_edge_index(DevGraph& g, uint32_t* status, cudaStream_t st)
+{
+    if (g.m == 0 || !g.eidx) return cudaSuccess;
+    k_edge_index<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj,
+                                                     reinterpret_cast<unsigned long long*>(g.eidx), g.eidx_cap, status);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_segmask(DevGraph& g, cudaStream_t st)
 {
     if (g.n == 0 || g.segw == 0) return cudaSuccess;
@@ -1277,6 +1380,9 @@ MaskDev mask_dev(const MaskArgs& x)
     a.segmask = x.g->segmask;
     a.selfloop = x.g->selfloop;
     a.rev = x.g->rev;
+    a.eidx = x.g->eidx;
+    a.eidx_cap = x.g->eidx_cap;
+    a.parallel = x.g->parallel;
     a.ecol = x.ecol;
     a.symmetric = x.g->symmetric;
     a.n = x.g->n;

@@ -44,3 +44,6 @@ def test_out_of_memory_leaves_context_usable():
         assert m.fsm(small, 3, 20)[0] == want
         got, _ = m.mine(dbig, 3, 10000)
         assert len(got) > 0
+        # What the failed runs freed is not kept from other processes.
+        free_b, total_b = torch.cuda.mem_get_info()
+        assert free_b > total_b // 2

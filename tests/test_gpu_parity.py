@@ -108,8 +108,10 @@ def test_fsm_cli_matches_golden():
     with tempfile.TemporaryDirectory() as tmp:
         path = os.path.join(tmp, "g.bin")
         g.save(path)
-        out = subprocess.run([os.path.join(ROOT, "gspan_gb300", "_lib", "fsm"), path, "20", "3"],
-                             capture_output=True, text=True, check=True).stdout.splitlines()
+        r = subprocess.run([os.path.join(ROOT, "gspan_gb300", "_lib", "fsm"), path, "20", "3"],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out = r.stdout.splitlines()
     assert out[-1].startswith("load:")
     assert out[:-1] == golden_lines(case)
 
