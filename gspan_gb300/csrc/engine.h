@@ -35,6 +35,7 @@ enum : uint32_t {
     kErrCursor = 1u << 2,       // a materialisation cursor ran past its reserved rows
     kErrAsymmetric = 1u << 3,   // upload: an entry without its reverse entry (not an error)
     kFlagParallel = 1u << 4,    // upload: two equal entries of one vertex (parallel edges; not an error)
+    kFlagSelfLoop = 1u << 5,    // upload: some vertex has an entry to itself (not an error)
 };
 
 // The graph in HBM.  Labels are replaced by their rank among the distinct
@@ -83,6 +84,9 @@ struct DevGraph {
     uint32_t eidx_cap = 0;
     // Some vertex has two equal entries (parallel edges with one label).
     bool parallel = true;
+    // Some vertex has an entry to itself.  Without self-loops every embedding
+    // maps distinct pattern vertices to distinct graph vertices.
+    bool loops = true;
     // Mean degree of a vertex reached through an edge (sum d^2 / sum d): the
     // expected adjacency length behind an embedding's vertex.
     double edge_biased_degree = 0;
@@ -140,6 +144,13 @@ struct ParentMeta {
     int8_t e_to[kMaxE];
     int16_t e_el[kMaxE];
     uint16_t src_adj[kMaxV];    // per source: pattern vertices joined to it by a code edge
+    // Pattern vertices in (stable) label order: equal labels are adjacent.
+    int8_t lorder[kMaxV];
+    // Per source and pattern vertex: the (last) code edge joining them, -1 if none.
+    int8_t pair_edge[kMaxV][kMaxV];
+    // Per backward target: bit el (el < 32) when a code edge with label el
+    // joins v_n and the target.
+    uint32_t back_used[kMaxV];
     // Materialisation: the frequent forward tuples as (source, el * nvl + tl),
     // scanned segment by segment; nmseg = -1 scans every source's full range.
     int16_t nmseg;

@@ -324,6 +324,7 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
         UP_CK(cudaStreamSynchronize(s), "graph flags");
         g.symmetric = !(flags & kErrAsymmetric);
+        g.loops = (flags & kFlagSelfLoop) != 0;
         g.entry_cols = g.symmetric && g.nel == 1;
     }
     // Edge index at a load factor in (3/8, 3/4].

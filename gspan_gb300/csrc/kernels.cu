@@ -706,6 +706,7 @@ struct MaskDev {
     int32_t ecol;
     bool symmetric;
     bool parallel;               // equal entries may follow each other
+    bool loops;                  // self-loops present: images of a row may repeat
     int32_t n, m, nvl, nel, mw, lwin;
     const ParentMeta* parents;
     int32_t nparents;
@@ -781,13 +782,14 @@ __global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const 
                               const uint64_t* __restrict__ adj, const int32_t* __restrict__ vrank,
                               uint32_t* __restrict__ selfloop, int32_t* __restrict__ rev, uint32_t* status)
 {
-    bool asym = false;
+    bool asym = false, loop = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t ent = adj[i];
         const uint32_t u = (uint32_t)src[i], x = entry_to(ent);
         if (u == x) {
             atomicOr(selfloop + (u >> 5), 1u << (u & 31));
             rev[i] = (int32_t)i;
+            loop = true;
             continue;
         }
         // Rank of i among the equal entries before it (parallel edges with one label).
@@ -801,7 +803,8 @@ __global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const 
         rev[i] = found ? q : -1;
         asym |= !found;
     }
-    if (__any_sync(kFull, asym) && (threadIdx.x & 31) == 0) atomicOr(status, kErrAsymmetric);
+    const unsigned am = __ballot_sync(kFull, asym), lm = __ballot_sync(kFull, loop);
+    if ((threadIdx.x & 31) == 0 && (am | lm)) atomicOr(status, (am ? kErrAsymmetric : 0u) | (lm ? kFlagSelfLoop : 0u));
 }
 
 // Thread per entry: the first entry of each run of equal entries goes into
@@ -901,23 +904,50 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
             if (a.ecol >= 0) {
                 // One edge label.  Images joined to the source by a pattern
                 // edge are found through the row's entry columns (or their
-                // reverse entries); the others by search, after a cheap
-                // existence test from the shorter side.
-                int32_t it_t[kMaxV], it_lb[kMaxV], it_ub[kMaxV];
-                int nit = 0;
+                // reverse entries); the others through the edge index (or by
+                // search, after a cheap existence test from the shorter side).
+                // Vertices are visited in label order, so each label's hits
+                // are summed on the fly: a segment is lost to the row when
+                // its images fill all of it.
                 const int vs = P.src_v[s];
-                for (int j = 0; j < nv; ++j) {
-                    const int t = P.vlab[j];
+                int cur_t = -1, gstart = 0;
+                int32_t hits = 0, minlb = e, maxub = b;
+                for (int oi = 0; oi <= nv; ++oi) {
+                    const int j = oi < nv ? P.lorder[oi] : 0;
+                    const int t = oi < nv ? P.vlab[j] : -1;
+                    if (t != cur_t) {
+                        if (hits > 0) {
+                            const uint32_t segk = (uint32_t)(pack_entry(0, (uint32_t)cur_t, 0) >> 32);
+                            const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
+                            const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
+                            if (first && last && maxub - minlb == hits) {
+                                const uint32_t kc = (uint32_t)(cur_t - P.lbase);
+#pragma unroll
+                                for (int w = 0; w < kMaxMaskWords; ++w)
+                                    ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
+                            }
+                        }
+                        cur_t = t;
+                        gstart = oi;
+                        hits = 0;
+                        minlb = e;
+                        maxub = b;
+                    }
+                    if (oi == nv) break;
                     const uint64_t seg0 = pack_entry(0, (uint32_t)t, 0);
                     if (t < min_label || seg0 < lo) continue;
                     const int32_t x = img[j];
-                    bool dup = false;
-                    for (int q = 0; q < j; ++q) dup |= img[q] == x;
-                    if (dup) continue;
+                    if (a.loops) {
+                        // Images may repeat: one hit per distinct image (equal
+                        // images have equal labels, so within the group).
+                        bool dup = false;
+                        for (int q = gstart; q < oi; ++q) dup |= img[P.lorder[q]] == x;
+                        if (dup) continue;
+                    } else if (j == vs) {
+                        continue;   // no self-loops: the source is not its own neighbour
+                    }
                     const uint64_t key = seg0 | (uint32_t)x;
-                    int jj = -1;
-                    for (int q = 0; q < P.nedge; ++q)
-                        if ((P.e_from[q] == vs && P.e_to[q] == j) || (P.e_to[q] == vs && P.e_from[q] == j)) jj = q;
+                    const int jj = P.pair_edge[s][j];
                     int32_t pos = -1;
                     if (jj >= 0) {
                         const int32_t stored = __ldg(a.in_cols[a.ecol + jj] + row);
@@ -948,31 +978,9 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                         while (ub < e && __ldg(a.adj + ub) == key) ++ub;
                     }
                     for (int32_t q = lb; q < ub; ++q) atomicAdd(Hs + q, 1u);
-                    it_t[nit] = t;
-                    it_lb[nit] = lb;
-                    it_ub[nit] = ub;
-                    ++nit;
-                }
-                // A segment is lost to the row when its images fill all of it.
-                for (int i = 0; i < nit; ++i) {
-                    bool lead = true;
-                    for (int q = 0; q < i; ++q) lead &= it_t[q] != it_t[i];
-                    if (!lead) continue;
-                    int32_t hits = 0, minlb = e, maxub = b;
-                    for (int q = i; q < nit; ++q) {
-                        if (it_t[q] != it_t[i]) continue;
-                        hits += it_ub[q] - it_lb[q];
-                        minlb = min(minlb, it_lb[q]);
-                        maxub = max(maxub, it_ub[q]);
-                    }
-                    const uint32_t segk = (uint32_t)(pack_entry(0, (uint32_t)it_t[i], 0) >> 32);
-                    const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
-                    const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
-                    if (first && last && maxub - minlb == hits) {
-                        const uint32_t kc = (uint32_t)(it_t[i] - P.lbase);
-#pragma unroll
-                        for (int w = 0; w < kMaxMaskWords; ++w) ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
-                    }
+                    hits += ub - lb;
+                    minlb = min(minlb, lb);
+                    maxub = max(maxub, ub);
                 }
             } else
             for (int el = 0; el < a.nel; ++el) {
@@ -987,9 +995,11 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                     for (int j = i; j < nv; ++j) {
                         if (P.vlab[j] != t) continue;
                         const int32_t x = img[j];
-                        bool dup = false;
-                        for (int q = i; q < j; ++q) dup |= img[q] == x;
-                        if (dup) continue;
+                        if (a.loops) {
+                            bool dup = false;
+                            for (int q = i; q < j; ++q) dup |= img[q] == x;
+                            if (dup) continue;
+                        }
                         // Most image pairs are not adjacent.  A vertex reaches
                         // itself only through a self-loop; a pair that the
                         // pattern does not join is first looked up from the
@@ -1067,11 +1077,18 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                         if (pos >= e || __ldg(a.adj + pos) != want) pos = -1;
                     }
                     if (pos >= 0) {
+                        // has_edge: the row already uses an edge (un, x, el).
+                        // Without self-loops images are distinct, so that is
+                        // a code edge joining v_n and the target.
                         bool used = false;
-                        for (int j = 0; j < P.nedge; ++j) {
-                            if (P.e_el[j] != el) continue;
-                            const int32_t f = img[P.e_from[j]], g2 = img[P.e_to[j]];
-                            if ((f == un && g2 == x) || (g2 == un && f == x)) used = true;
+                        if (!a.loops && el < 32) {
+                            used = (P.back_used[t] >> el) & 1u;
+                        } else {
+                            for (int j = 0; j < P.nedge; ++j) {
+                                if (P.e_el[j] != el) continue;
+                                const int32_t f = img[P.e_from[j]], g2 = img[P.e_to[j]];
+                                if ((f == un && g2 == x) || (g2 == un && f == x)) used = true;
+                            }
                         }
                         if (!used) {
                             ok = true;
@@ -1383,6 +1400,7 @@ MaskDev mask_dev(const MaskArgs& x)
     a.eidx = x.g->eidx;
     a.eidx_cap = x.g->eidx_cap;
     a.parallel = x.g->parallel;
+    a.loops = x.g->loops;
     a.ecol = x.ecol;
     a.symmetric = x.g->symmetric;
     a.n = x.g->n;

@@ -526,6 +526,18 @@ struct Run {
                 P.e_to[j] = (int8_t)c[j].to;
                 P.e_el[j] = (int16_t)c[j].el;
             }
+            for (int j = 0; j < nv; ++j) P.lorder[j] = (int8_t)j;
+            std::stable_sort(P.lorder, P.lorder + nv, [&](int8_t x, int8_t y) { return P.vlab[x] < P.vlab[y]; });
+            std::memset(P.pair_edge, -1, sizeof(P.pair_edge));
+            for (int s2 = 0; s2 < P.nsrc; ++s2)
+                for (size_t q = 0; q < c.size(); ++q) {
+                    if (c[q].from == P.src_v[s2]) P.pair_edge[s2][c[q].to] = (int8_t)q;
+                    if (c[q].to == P.src_v[s2]) P.pair_edge[s2][c[q].from] = (int8_t)q;
+                }
+            for (int t = 0; t < P.nback; ++t)
+                for (const CodeEdge& e : c)
+                    if (e.el < 32 && ((e.from == P.vn && e.to == P.back_v[t]) || (e.to == P.vn && e.from == P.back_v[t])))
+                        P.back_used[t] |= 1u << e.el;
             P.row_begin = parents[i].row_begin;
             P.row_end = parents[i].row_end;
             P.key_base = (int32_t)nkeys;
