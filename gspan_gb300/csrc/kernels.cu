@@ -370,10 +370,15 @@ __global__ void k_seed_count(int32_t m, const int32_t* __restrict__ src, const u
         int32_t key = 0;
         uint32_t u, w;
         const bool ok = i < m && seed_key(src, adj, vrank, win_base, lwin, nel, i, &key, &u, &w);
-        const unsigned mask = __ballot_sync(kFull, ok);
-        if (ok) {
-            const unsigned peers = __match_any_sync(mask, key);
-            if (lane == __ffs(peers) - 1) atomicAdd(counts + key, (unsigned long long)__popc(peers));
+        // Entries are sorted per vertex, so equal keys come in runs of
+        // consecutive lanes: one atomic per run (`ok` is a function of the key).
+        const unsigned okm = __ballot_sync(kFull, ok);
+        const int32_t prev = __shfl_up_sync(kFull, key, 1);
+        const unsigned heads = __ballot_sync(kFull, ok && (lane == 0 || !((okm >> (lane - 1)) & 1u) || prev != key));
+        if ((heads >> lane) & 1u) {
+            const unsigned stop = (heads | ~okm) & ~((2u << lane) - 1u);
+            const int end = stop ? __ffs(stop) - 1 : 32;
+            atomicAdd(counts + key, (unsigned long long)(end - lane));
         }
     }
 }
@@ -395,20 +400,28 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
         bool ok = i < m && seed_key(src, adj, vrank, win_base, lwin, nel, i, &key, &u, &w);
         const int32_t a = ok ? keys.act[key] : -1;
         ok = a >= 0;
+        // Runs of consecutive lanes with equal (active key, source vertex):
+        // the source goes into its domain once per run.
+        const unsigned okm = __ballot_sync(kFull, ok);
+        const uint64_t rk = ((uint64_t)(uint32_t)a << 32) | u;
+        const uint64_t prev = __shfl_up_sync(kFull, rk, 1);
+        const unsigned heads = __ballot_sync(kFull, ok && (lane == 0 || !((okm >> (lane - 1)) & 1u) || prev != rk));
         if (ok) {
             const DomDesc d = keys.dom[a];
-            dom_insert(pool, d, 0, u, status);
+            if ((heads >> lane) & 1u) dom_insert(pool, d, 0, u, status);
             dom_insert(pool, d, 1, w, status);
         }
         const bool mat = ok && keys.mat_off[a] >= 0;
         const unsigned mm = __ballot_sync(kFull, mat);
         if (mat) {
-            const unsigned peers = __match_any_sync(mm, a);
-            const int leader = __ffs(peers) - 1;
+            // One cursor reservation per run (materialisation depends on the key only).
+            const int h = 31 - __clz(heads & ((2u << lane) - 1u));
+            const unsigned stop = (heads | ~mm) & ~((2u << h) - 1u);
+            const int end = stop ? __ffs(stop) - 1 : 32;
             unsigned long long at = 0;
-            if (lane == leader) at = atomicAdd(keys.cursor + a, (unsigned long long)__popc(peers));
-            at = __shfl_sync(mm, at, leader);
-            const unsigned long long slot = at + __popc(peers & lanemask_lt());
+            if (lane == h) at = atomicAdd(keys.cursor + a, (unsigned long long)(end - h));
+            at = __shfl_sync(mm, at, h);
+            const unsigned long long slot = at + (unsigned long long)(lane - h);
             if (slot < keys.counts[key]) {
                 const long long row = keys.mat_off[a] + (long long)slot;
                 col0[row] = (int32_t)u;
