@@ -61,6 +61,12 @@ def workloads():
         "chung_lu_100k_s15k": dict(
             make=lambda: datagen.chung_lu_100k(1), min_support=15000, k=3, sample_k=2,
             desc="Chung-Lu 100,000 V / 1,080,000 E (as chung_lu_100k), min support 15,000"),
+        # The large single graph, at 3 edges: its 4-edge level needs a level-3
+        # embedding table of about 1.1e12 rows, beyond the device.
+        "chung_lu_3_7m": dict(
+            make=lambda: datagen.chung_lu_3_7m(3), min_support=20000, k=3, sample_k=None,
+            desc="Chung-Lu 3,700,000 V / 16,500,000 E, exponent 2.3, degree cap sqrt(2m), 37 vertex labels "
+                 "Zipf(0.8), 1 edge label, seed 3"),
         "er_3300": dict(
             make=lambda: datagen.er_3300(0), min_support=20, k=3, sample_k=3,
             desc="Erdos-Renyi 3,300 V / 4,700 E, 6 uniform vertex labels, 1 edge label, seed 0"),
@@ -164,6 +170,10 @@ def reference_arm(args, wl) -> None:
     world, rank, _ = dist_setup()
     if rank != 0:
         return
+    if wl["sample_k"] is None:
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU port would hold about 1e10 two-edge "
+                                                              "embeddings of this graph in host memory"}), flush=True)
+        return
     cores = host_cores()
     g = wl["make"]()
     with tempfile.TemporaryDirectory() as tmp:
@@ -218,7 +228,9 @@ def gpu_arm(args, wl) -> None:
     h2d_graph = off_h.numel() * 4 + vl_h.numel() * 4 + ed_h.numel() * 4
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if wl["sample_k"] is None:
+        cpu = {"unavailable": "the CPU port would hold about 1e10 two-edge embeddings of this graph in host memory"}
+    elif rank == 0 and world == 1 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as tmp:
             path = os.path.join(tmp, "g.bin")
             g.save(path)

@@ -89,16 +89,13 @@ gspan_status gspan_ctx_create(const gspan_opts* opts, gspan_ctx** out)
         if ((e = cudaEventCreate(ev)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&ctx->d_status, 4)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&ctx->d_counters, 32)) != cudaSuccess) return bail(e);
-    // Keep up to an eighth of the device's memory of freed stream-ordered
-    // blocks cached in this process, so the per-level buffers of repeated
-    // mining runs do not go back to the driver; what a very large run freed
-    // beyond that is released at the next synchronisation, for other
-    // processes.
+    // Keep freed stream-ordered blocks cached in this process, so the
+    // per-level buffers of repeated mining runs are not mapped again each
+    // run.  A run that fails for want of memory gives the cache back (see
+    // gs::mine).
     cudaMemPool_t pool;
-    size_t free_b = 0, total_b = 0;
-    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess &&
-        cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-        uint64_t keep = total_b / 8;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     cudaGetLastError();

@@ -114,11 +114,20 @@ void dfree(T*& p, cudaStream_t st)
 struct LiveBlocks {
     std::unordered_set<void*> blocks;
     cudaStream_t s;
-    explicit LiveBlocks(cudaStream_t st) : s(st) { t_live = &blocks; }
+    int device;
+    bool out_of_memory = false;
+    LiveBlocks(cudaStream_t st, int dev) : s(st), device(dev) { t_live = &blocks; }
     ~LiveBlocks()
     {
         for (void* p : blocks) cudaFreeAsync(p, s);
         t_live = nullptr;
+        // A run that ran out of memory has grown the pool to the device's
+        // limit: hand the unused part back, so other work (and other
+        // processes) can allocate again.
+        cudaMemPool_t pool;
+        if (out_of_memory && cudaStreamSynchronize(s) == cudaSuccess &&
+            cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess)
+            cudaMemPoolTrimTo(pool, 0);
     }
 };
 
@@ -968,7 +977,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<in
     // set-up); here it is an argument error.
     if (k < 1) return fail(ctx, GSPAN_ERR_INVALID, "k must be at least 1");
     if (k > kMaxE) return fail(ctx, GSPAN_ERR_LIMIT, "k exceeds the largest supported pattern size");
-    LiveBlocks live(ctx->stream);
+    LiveBlocks live(ctx->stream, ctx->device);
     Run run{ctx, g, k, minsup};
     run.s = ctx->stream;
     run.profile = ctx->opts.profile != 0;
@@ -995,6 +1004,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<in
     run.drop_events();
     run.st.levels = run.found.empty() ? 0 : size;
     if (rc != GSPAN_OK) {
+        live.out_of_memory = rc == GSPAN_ERR_NOMEM;
         cudaStreamSynchronize(run.s);
         return rc;
     }
