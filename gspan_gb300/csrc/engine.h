@@ -184,6 +184,7 @@ enum class Pass : int { Count = 0, Support = 1, Materialize = 2 };
 struct ExpandArgs {
     const DevGraph* g;                 // host copy; device pointers inside are used
     const ParentMeta* parents;         // device
+    const ParentMeta* parents_h;       // host copy of the same parents (sizes the launch's scratch)
     int32_t nparents;
     int64_t ntiles;
     int32_t in_cols;                   // columns of the parent table

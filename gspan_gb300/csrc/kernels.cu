@@ -449,6 +449,7 @@ struct ExpandDev {
     int32_t* const* in_cols;
     int32_t* const* out_cols;
     int32_t ecol_in, ecol_out;   // first entry column of the parent / child table (-1: none)
+    int32_t vs, ss;              // scratch strides: >= every parent's vertices / ranges, odd
     LevelKeys keys;
     uint32_t* pool;
     unsigned long long* tile_counter;
@@ -456,18 +457,21 @@ struct ExpandDev {
     uint32_t* status;
 };
 
-struct WarpScratch {
-    int32_t img[32][kMaxV + 1];   // this tile's row images, one row per lane
-    int32_t start[32][kMaxV];     // per row and source: first adjacency entry in range
-    int32_t cnt[32][kMaxV];       // per row and source: entries in range
-    int32_t pre[32];              // exclusive prefix of the rows' entry counts
-};
+// Per-warp scratch in dynamic shared memory, sized per launch by the level's
+// largest parent: img [32][vs] (row images, one row per lane), start and cnt
+// [32][ss] (per row and range: first adjacency entry, entries), pre [32]
+// (exclusive prefix of the rows' entry counts).  vs, ss are odd (no bank
+// conflicts between lanes).
+__host__ __device__ inline int expand_warp_ints(int vs, int ss) { return 32 * (vs + 2 * ss + 1); }
 
 template <Pass kPass>
 __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    WarpScratch& W = reinterpret_cast<WarpScratch*>(smem_raw)[threadIdx.x >> 5];
+    int32_t* const Wimg = reinterpret_cast<int32_t*>(smem_raw) + (threadIdx.x >> 5) * expand_warp_ints(a.vs, a.ss);
+    int32_t* const Wstart = Wimg + 32 * a.vs;
+    int32_t* const Wcnt = Wstart + 32 * a.ss;
+    int32_t* const Wpre = Wcnt + 32 * a.ss;
     const int lane = threadIdx.x & 31;
     const int32_t LeLv = a.nel * a.lwin;
 
@@ -490,7 +494,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
         const int64_t row = P.row_begin + (tile - P.tile_begin) * 32 + lane;
         const bool live = row < P.row_end;
 
-        for (int p = 0; p < nv; ++p) W.img[lane][p] = live ? __ldcs(a.in_cols[p] + row) : -1;
+        for (int p = 0; p < nv; ++p) Wimg[(lane) * a.vs + (p)] = live ? __ldcs(a.in_cols[p] + row) : -1;
 
         // Ranges to scan per row: one per source (the source's valid suffix),
         // or, when materialising with few frequent tuples, one per frequent
@@ -502,7 +506,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
             int32_t st = 0, c = 0;
             if (live) {
                 const int sq = segs ? P.mseg_s[q] : q;
-                const int32_t u = W.img[lane][P.src_v[sq]];
+                const int32_t u = Wimg[(lane) * a.vs + (P.src_v[sq])];
                 const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
                 if (segs) {
                     const uint32_t el = P.mseg_kc[q] / (uint32_t)a.lwin;
@@ -516,8 +520,8 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                     c = e - st;
                 }
             }
-            W.start[lane][q] = st;
-            W.cnt[lane][q] = c;
+            Wstart[(lane) * a.ss + (q)] = st;
+            Wcnt[(lane) * a.ss + (q)] = c;
             work += c;
         }
         int32_t incl = work;
@@ -526,7 +530,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
             const int32_t t = __shfl_up_sync(kFull, incl, d);
             if (lane >= d) incl += t;
         }
-        W.pre[lane] = incl - work;
+        Wpre[lane] = incl - work;
         const int32_t total = __shfl_sync(kFull, incl, 31);
         __syncwarp();
         if (kPass != Pass::Support && lane == 0 && total > 0)
@@ -539,8 +543,8 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
             int32_t bpos = 0;   // entry index of the backward edge found
             if (live) {
                 const int bv = P.back_v[t];
-                const int32_t x = W.img[lane][bv];
-                const int32_t un = W.img[lane][P.vn];
+                const int32_t x = Wimg[(lane) * a.vs + (bv)];
+                const int32_t un = Wimg[(lane) * a.vs + (P.vn)];
                 const uint32_t tlx = (uint32_t)P.vlab[bv];
                 const int32_t b = __ldg(a.offsets + un), e = __ldg(a.offsets + un + 1);
                 for (int32_t el = P.back_eq[t] ? P.back_el[t] : P.back_el[t] + 1; el < a.nel && !ok; ++el) {
@@ -556,7 +560,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                         bool used = false;
                         for (int j = 0; j < P.nedge; ++j) {
                             if (P.e_el[j] != el) continue;
-                            const int32_t f = W.img[lane][P.e_from[j]], g2 = W.img[lane][P.e_to[j]];
+                            const int32_t f = Wimg[(lane) * a.vs + (P.e_from[j])], g2 = Wimg[(lane) * a.vs + (P.e_to[j])];
                             if ((f == un && g2 == x) || (g2 == un && f == x)) used = true;
                         }
                         if (!used) {
@@ -579,7 +583,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                 const bool sup = ai >= 0;
                 if (kPass == Pass::Support && sup) {
                     const DomDesc d = a.keys.dom[ai];
-                    for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)W.img[lane][p], a.status);
+                    for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)Wimg[(lane) * a.vs + (p)], a.status);
                 }
                 const bool mat = kPass == Pass::Materialize && sup;
                 const unsigned mm = __ballot_sync(kFull, mat);
@@ -592,7 +596,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                     const unsigned long long slot = at + __popc(peers & lanemask_lt());
                     if (slot < a.keys.counts[key]) {
                         const long long r = a.keys.mat_off[ai] + (long long)slot;
-                        for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[lane][p];
+                        for (int p = 0; p < nv; ++p) a.out_cols[p][r] = Wimg[(lane) * a.vs + (p)];
                         if (a.ecol_out >= 0) {
                             for (int j = 0; j < P.nedge; ++j)
                                 a.out_cols[a.ecol_out + j][r] = __ldg(a.in_cols[a.ecol_in + j] + row);
@@ -617,21 +621,21 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                 int l2 = 0, h2 = 31;
                 while (l2 < h2) {
                     const int mid = (l2 + h2 + 1) >> 1;
-                    if (W.pre[mid] <= item) l2 = mid; else h2 = mid - 1;
+                    if (Wpre[mid] <= item) l2 = mid; else h2 = mid - 1;
                 }
                 owner = l2;
-                int32_t j = item - W.pre[owner];
+                int32_t j = item - Wpre[owner];
                 int s = 0;
-                while (j >= W.cnt[owner][s]) {
-                    j -= W.cnt[owner][s];
+                while (j >= Wcnt[(owner) * a.ss + (s)]) {
+                    j -= Wcnt[(owner) * a.ss + (s)];
                     ++s;
                 }
-                eidx = W.start[owner][s] + j;
+                eidx = Wstart[(owner) * a.ss + (s)] + j;
                 const uint64_t e = __ldg(a.adj + eidx);
                 to = entry_to(e);
                 const int32_t tl = (int32_t)entry_tl(e);
                 bool fresh = tl >= min_label && (uint32_t)(tl - P.lbase) < (uint32_t)a.lwin;
-                for (int p = 0; p < nv; ++p) fresh &= W.img[owner][p] != (int32_t)to;
+                for (int p = 0; p < nv; ++p) fresh &= Wimg[(owner) * a.vs + (p)] != (int32_t)to;
                 ok = fresh;
                 key = key_base + (segs ? P.mseg_s[s] : s) * LeLv + (int32_t)entry_el(e) * a.lwin + (tl - P.lbase);
             }
@@ -652,7 +656,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                         // The parent row's images go in once per (row, child tuple) in this chunk.
                         const unsigned peers = __match_any_sync(sm, ((unsigned long long)owner << 32) | (unsigned)ai);
                         if (lane == __ffs(peers) - 1)
-                            for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)W.img[owner][p], a.status);
+                            for (int p = 0; p < nv; ++p) dom_insert(a.pool, d, p, (uint32_t)Wimg[(owner) * a.vs + (p)], a.status);
                     }
                 }
                 const bool mat = kPass == Pass::Materialize && sup;
@@ -666,7 +670,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                     const unsigned long long slot = at + __popc(peers & lanemask_lt());
                     if (slot < a.keys.counts[key]) {
                         const long long r = a.keys.mat_off[ai] + (long long)slot;
-                        for (int p = 0; p < nv; ++p) a.out_cols[p][r] = W.img[owner][p];
+                        for (int p = 0; p < nv; ++p) a.out_cols[p][r] = Wimg[(owner) * a.vs + (p)];
                         a.out_cols[nv][r] = (int32_t)to;
                         if (a.ecol_out >= 0) {
                             const int64_t orow = P.row_begin + (tile - P.tile_begin) * 32 + owner;
@@ -1327,9 +1331,10 @@ cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* poo
 
 int expand_grid_blocks(int device)
 {
+    // Allow the largest scratch (kMaxV vertices and ranges) on this device.
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const size_t smem = sizeof(WarpScratch) * kExpandWarps;
+    const size_t smem = (size_t)kExpandWarps * 4 * expand_warp_ints(kMaxV | 1, kMaxV | 1);
     cudaFuncSetAttribute(k_expand<Pass::Count>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_expand<Pass::Support>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_expand<Pass::Materialize>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1361,13 +1366,28 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     a.tile_counter = x.tile_counter;
     a.scanned = x.scanned;
     a.status = x.status;
-    int dev = 0;
+    // Scratch strides from the largest parent of this launch.
+    int maxv = 1, maxs = 1;
+    for (int32_t i = 0; i < x.nparents; ++i) {
+        const ParentMeta& P = x.parents_h[i];
+        maxv = std::max(maxv, (int)P.nv);
+        maxs = std::max(maxs, pass == Pass::Materialize && P.nmseg >= 0 ? (int)P.nmseg : (int)P.nsrc);
+    }
+    a.vs = maxv | 1;
+    a.ss = maxs | 1;
+    const size_t smem = (size_t)kExpandWarps * 4 * expand_warp_ints(a.vs, a.ss);
+    int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
-    static int blocks[64] = {0};
-    if (blocks[dev] == 0) blocks[dev] = expand_grid_blocks(dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (pass == Pass::Count)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_expand<Pass::Count>, kExpandThreads, smem);
+    else if (pass == Pass::Support)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_expand<Pass::Support>, kExpandThreads, smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_expand<Pass::Materialize>, kExpandThreads, smem);
+    const int64_t cap = (int64_t)sms * std::max(per_sm, 1);
     const int64_t need = (x.ntiles + kExpandWarps - 1) / kExpandWarps;
-    const int grid = (int)(need < blocks[dev] ? need : blocks[dev]);
-    const size_t smem = sizeof(WarpScratch) * kExpandWarps;
+    const int grid = (int)(need < cap ? need : cap);
     if (pass == Pass::Count)
         k_expand<Pass::Count><<<grid, kExpandThreads, smem, st>>>(a);
     else if (pass == Pass::Support)

@@ -756,6 +756,7 @@ struct Run {
             GS_CK(dalloc(&d_cg, cg.size(), s), "alloc parents");
             GS_CK(copy(d_cg, cg.data(), cg.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
             x.parents = d_cg;
+            x.parents_h = cg.data();
             x.nparents = (int32_t)cg.size();
             x.ntiles = ctiles;
             tic(&e0, &e1);
@@ -846,6 +847,7 @@ struct Run {
             }
             GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 8, s), "clear tile counter");
             x.parents = d_cg;
+            x.parents_h = cg.data();
             x.nparents = (int32_t)cg.size();
             x.ntiles = ctiles;
             x.keys = LevelKeys{d_counts, as.d_act, as.d_dom, as.d_mat, as.d_cursor};
@@ -936,6 +938,7 @@ struct Run {
         GS_CK(copy(d_all, all.data(), all.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
         GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 16, s), "clear counters");
         x.parents = d_all;
+        x.parents_h = all.data();
         x.nparents = (int32_t)all.size();
         x.ntiles = atiles;
         x.keys = LevelKeys{d_counts, d_act, nullptr, d_mat, d_cur};
