@@ -73,7 +73,8 @@ class Stats(ctypes.Structure):
                 ("sweep_ms", ctypes.c_double), ("sweep_bytes", ctypes.c_double),
                 ("materialize_ms", ctypes.c_double), ("materialize_launches", ctypes.c_uint64),
                 ("materialize_bytes", ctypes.c_double),
-                ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double)]
+                ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double),
+                ("canonical_checks", ctypes.c_uint64), ("canonical_ms", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

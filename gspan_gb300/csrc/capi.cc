@@ -89,6 +89,7 @@ gspan_status gspan_ctx_create(const gspan_opts* opts, gspan_ctx** out)
         if ((e = cudaEventCreate(ev)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&ctx->d_status, 4)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&ctx->d_counters, 32)) != cudaSuccess) return bail(e);
+    if ((e = cudaMallocHost(&ctx->h_pin, 64)) != cudaSuccess) return bail(e);
     // Keep freed stream-ordered blocks cached in this process, so the
     // per-level buffers of repeated mining runs are not mapped again each
     // run.  A run that fails for want of memory gives the cache back (see
@@ -111,6 +112,7 @@ void gspan_ctx_destroy(gspan_ctx* ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     for (cudaEvent_t ev : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d})
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -480,6 +480,32 @@ struct Run {
         int support;
     };
 
+    // Materialisation readback waiting for a sync (see the end of level()).
+    bool pending_scan = false;
+    void settle()
+    {
+        if (!pending_scan) return;
+        st.scanned_entries += ctx->h_pin[0];
+        st.materialize_bytes += 8.0 * (double)ctx->h_pin[0];
+        pending_scan = false;
+    }
+
+    // The code of child tuple lk (parent-local key) of a parent with code c.
+    void child_of(const std::vector<CodeEdge>& c, const ParentMeta& P, int64_t lk, std::vector<CodeEdge>& child) const
+    {
+        const int32_t K = g.nel * g.lwin;
+        child = c;
+        if (lk < (int64_t)P.nsrc * K) {
+            const int s2 = (int)(lk / K);
+            const int el = (int)((lk % K) / g.lwin);
+            const int tl = P.lbase + (int)(lk % g.lwin);
+            child.push_back(CodeEdge{P.src_v[s2], P.nv, -1, el, tl});
+        } else {
+            const int64_t r = lk - (int64_t)P.nsrc * K;
+            child.push_back(CodeEdge{P.vn, P.back_v[(int)(r / g.nel)], -1, (int)(r % g.nel), -1});
+        }
+    }
+
     gspan_status level(int size, std::vector<Parent>& parents, Table& table, std::vector<Parent>& next, Table& out)
     {
         const int32_t K = g.nel * g.lwin;
@@ -765,20 +791,39 @@ struct Run {
             ++st.kernel_launches;
             ++st.expand_launches;
         }
+        // A child's code does not depend on its counts: while the GPU
+        // counts, test the level's child tuples for minimum codes on the
+        // host, stopping as soon as the stream is done so the GPU never
+        // waits for it.  The decision below tests what is left.
+        std::vector<int8_t> canon((size_t)nkeys, -1);
+        {
+            std::vector<CodeEdge> child;
+            bool busy = true;
+            for (int i = 0; i < np && busy; ++i)
+                for (int64_t lk = 0; lk < key_span[i]; ++lk) {
+                    if ((lk & 15) == 0 && cudaStreamQuery(s) != cudaErrorNotReady) {
+                        busy = false;
+                        break;
+                    }
+                    child_of(parents[i].code, meta[i], lk, child);
+                    canon[(size_t)(meta[i].key_base + lk)] = is_min_code(child.data(), (int)child.size()) ? 1 : 0;
+                }
+            if (cudaPeekAtLastError() == cudaErrorNotReady) cudaGetLastError();
+        }
         std::vector<unsigned long long> counts((size_t)nkeys);
         std::vector<uint32_t> sizes((size_t)sz_total);
         unsigned long long ctr[4] = {0, 0, 0, 0};
+        uint32_t mstat = 0;
         GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read counts");
         if (sz_total) GS_CK(copy(sizes.data(), d_sizes, sz_total * 4, cudaMemcpyDeviceToHost, s), "read sizes");
         GS_CK(copy(ctr, ctx->d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s), "read counters");
+        GS_CK(copy(&mstat, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
         GS_CK(cudaStreamSynchronize(s), "extension count");
         resolve();
+        settle();
         st.scanned_entries += ctr[1] + ctr[3];
         if (!cg.empty()) st.expand_bytes += cand_read_bytes + 8.0 * (double)ctr[1];
         if (!groups.empty()) st.sweep_bytes += 12.0 * (double)ctr[3];
-        uint32_t mstat = 0;
-        GS_CK(copy(&mstat, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
-        GS_CK(cudaStreamSynchronize(s), "read status");
         if (mstat) return fail(ctx, GSPAN_ERR_DEVICE, "kernel status word " + std::to_string(mstat));
         // The mask kernels are done with their arrays.
         dfree(d_R, s);
@@ -800,28 +845,22 @@ struct Run {
                 if (cnt == 0) continue;
                 st.extended += cnt;
                 if (cnt < threshold(c[0].fl)) continue;
-                std::vector<CodeEdge> child = c;
-                int nvc;
-                int64_t size_at;
-                int stride;
-                if (lk < (int64_t)P.nsrc * K) {
-                    const int s2 = (int)(lk / K);
-                    const int el = (int)((lk % K) / g.lwin);
-                    const int tl = P.lbase + (int)(lk % g.lwin);
-                    child.push_back(CodeEdge{P.src_v[s2], P.nv, -1, el, tl});
-                    nvc = P.nv + 1;
-                    size_at = sz_off[i] + lk * (P.nv + 1);
-                    stride = 1;
-                } else {
-                    const int64_t r = lk - (int64_t)P.nsrc * K;
-                    const int t = (int)(r / g.nel);
-                    const int el = (int)(r % g.nel);
-                    child.push_back(CodeEdge{P.vn, P.back_v[t], -1, el, -1});
-                    nvc = P.nv;
-                    size_at = sz_off[i] + (int64_t)P.nsrc * K * (P.nv + 1) + r * P.nv;
-                    stride = 1;
+                std::vector<CodeEdge> child;
+                child_of(c, P, lk, child);
+                const bool fwd = lk < (int64_t)P.nsrc * K;
+                const int nvc = fwd ? P.nv + 1 : P.nv;
+                const int64_t size_at = fwd ? sz_off[i] + lk * (P.nv + 1)
+                                            : sz_off[i] + (int64_t)P.nsrc * K * (P.nv + 1) +
+                                                  (lk - (int64_t)P.nsrc * K) * P.nv;
+                const int stride = 1;
+                ++st.canonical_checks;
+                int8_t cf = canon[(size_t)key];
+                if (cf < 0) {
+                    const auto c0 = Clock::now();
+                    cf = is_min_code(child.data(), (int)child.size()) ? 1 : 0;
+                    st.canonical_ms += std::chrono::duration<double, std::milli>(Clock::now() - c0).count();
                 }
-                if (!is_min_code(child.data(), (int)child.size())) continue;
+                if (!cf) continue;
                 if (use_mask[i]) {
                     uint32_t best = std::numeric_limits<uint32_t>::max();
                     for (int p = 0; p < nvc; ++p) {
@@ -949,18 +988,16 @@ struct Run {
         toc(e0, e1, &st.materialize_ms);
         ++st.kernel_launches;
         ++st.materialize_launches;
-        unsigned long long scanned = 0;
-        GS_CK(copy(&scanned, ctx->d_counters + 1, 8, cudaMemcpyDeviceToHost, s), "read counters");
-        uint32_t mstatus = 0;
-        GS_CK(copy(&mstatus, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
-        GS_CK(cudaStreamSynchronize(s), "materialise");
-        resolve();
-        if (mstatus) return fail(ctx, GSPAN_ERR_DEVICE, "kernel status word " + std::to_string(mstatus));
-        st.scanned_entries += scanned;
+        // No sync here: the next level's host work overlaps this pass.  Its
+        // status bits are read with the next level's counts (the status
+        // word accumulates over the run) and its scanned-entry counter lands
+        // in pinned memory, settled after that sync.
+        GS_CK(copy(ctx->h_pin, ctx->d_counters + 1, 8, cudaMemcpyDeviceToHost, s), "read counters");
+        pending_scan = true;
         st.materialized_rows += (uint64_t)rows;
         double wbytes = 0;
         for (const Freq& f : freq) wbytes += 4.0 * f.nvc * (double)f.count;
-        st.materialize_bytes += all_read_bytes + 8.0 * (double)scanned + wbytes;
+        st.materialize_bytes += all_read_bytes + wbytes;
         for (size_t a2 = 0; a2 < freq.size(); ++a2)
             next.push_back(Parent{freq[a2].code, mat_h[a2], mat_h[a2] + (int64_t)freq[a2].count});
         dfree(d_act, s);
@@ -1012,6 +1049,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<in
         return rc;
     }
     GS_CK(cudaStreamSynchronize(run.s), "mine");
+    run.settle();
 
     std::sort(run.found.begin(), run.found.end(),
               [](const Found& a, const Found& b) { return preorder_less(a.code, b.code); });

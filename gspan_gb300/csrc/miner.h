@@ -38,6 +38,8 @@ struct gspan_ctx {
     // Small device words reused by every pass.
     uint32_t* d_status = nullptr;
     unsigned long long* d_counters = nullptr;   // [0],[2] tile counters, [1],[3] scanned entries
+    // Pinned host words for readbacks that are settled at a later sync.
+    unsigned long long* h_pin = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_c = nullptr, ev_d = nullptr;
     int live_graphs = 0;
 };

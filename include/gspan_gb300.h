@@ -97,6 +97,8 @@ typedef struct gspan_stats {
     double materialize_bytes;
     double seed_ms;
     double domain_ms;            /* domain-size reductions */
+    uint64_t canonical_checks;   /* children that needed the minimum-code test (host) */
+    double canonical_ms;         /* host time in tests not already done while the GPU counted */
 } gspan_stats;
 
 typedef struct gspan_ctx gspan_ctx;
