@@ -63,6 +63,8 @@ struct DevGraph {
     // space nel * nvl fits kMaxMaskWords words, else null (segw = 0).
     uint32_t* segmask = nullptr;
     int32_t segw = 0;
+    // Same layout: bit set when that segment holds exactly one entry.
+    uint32_t* segone = nullptr;
     // Bit v set when vertex v has an entry to itself.
     uint32_t* selfloop = nullptr;
     // Every entry u->x with edge label l has a reverse entry x->u with label l

@@ -67,6 +67,8 @@ void free_graph(gspan_graph* gr, cudaStream_t st)
     if (g.src) cudaFreeAsync(g.src, st);
     if (g.vrank) cudaFreeAsync(g.vrank, st);
     if (g.segmask) cudaFreeAsync(g.segmask, st);
+    if (g.segone) cudaFreeAsync(g.segone, st);
+    g.segone = nullptr;
     if (g.selfloop) cudaFreeAsync(g.selfloop, st);
     if (g.rev) cudaFreeAsync(g.rev, st);
     g.rev = nullptr;
@@ -300,6 +302,7 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         if (N > 0 && K > 0 && K <= 32 * kMaxMaskWords) {
             g.segw = (int32_t)((K + 31) / 32);
             UP_CK(cudaMallocAsync(&g.segmask, (size_t)N * g.segw * 4, s), "alloc segment masks");
+            UP_CK(cudaMallocAsync(&g.segone, (size_t)N * g.segw * 4, s), "alloc segment masks");
             UP_CK(launch_segmask(g, s), "segment mask launch");
         }
     }

@@ -716,6 +716,7 @@ struct MaskDev {
     const int32_t* offsets;
     const uint64_t* adj;
     const uint32_t* segmask;
+    const uint32_t* segone;      // segments of exactly one entry
     const uint32_t* selfloop;
     const int32_t* rev;
     const uint64_t* eidx;        // edge index (null: binary search)
@@ -772,24 +773,38 @@ __device__ __forceinline__ void add_fresh_bits(uint32_t fresh, uint32_t* sizes, 
 
 __global__ void k_segmask(int32_t n, int32_t lwin, int32_t segw, const int32_t* __restrict__ vrank,
                           const int32_t* __restrict__ win_base, const int32_t* __restrict__ offsets,
-                          const uint64_t* __restrict__ adj, uint32_t* __restrict__ segmask)
+                          const uint64_t* __restrict__ adj, uint32_t* __restrict__ segmask,
+                          uint32_t* __restrict__ segone)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t v = warp; v < n; v += nwarps) {
-        uint32_t w[kMaxMaskWords] = {0, 0, 0, 0};
+        uint32_t w[kMaxMaskWords] = {0, 0, 0, 0}, one[kMaxMaskWords] = {0, 0, 0, 0};
         const uint32_t wb = (uint32_t)win_base[vrank[v]];
-        for (int32_t j = offsets[v] + lane; j < offsets[v + 1]; j += 32) {
+        const int32_t b = offsets[v], e = offsets[v + 1];
+        for (int32_t j = b + lane; j < e; j += 32) {
             const uint64_t ent = adj[j];
+            const uint32_t seg = (uint32_t)(ent >> 32);   // (edge label, to label)
             const uint32_t kc = entry_el(ent) * (uint32_t)lwin + entry_tl(ent) - wb;
+            // Entries are sorted by segment: a singleton differs from both neighbours.
+            const bool single = (j == b || (uint32_t)(adj[j - 1] >> 32) != seg) &&
+                                (j + 1 == e || (uint32_t)(adj[j + 1] >> 32) != seg);
 #pragma unroll
-            for (int i = 0; i < kMaxMaskWords; ++i) w[i] |= (uint32_t)(i == (int)(kc >> 5)) << (kc & 31u);
+            for (int i = 0; i < kMaxMaskWords; ++i) {
+                const uint32_t bit = (uint32_t)(i == (int)(kc >> 5)) << (kc & 31u);
+                w[i] |= bit;
+                one[i] |= single ? bit : 0u;
+            }
         }
 #pragma unroll
         for (int i = 0; i < kMaxMaskWords; ++i) {
             const uint32_t r = __reduce_or_sync(kFull, w[i]);
-            if (lane == 0 && i < segw) segmask[v * segw + i] = r;
+            const uint32_t r1 = __reduce_or_sync(kFull, one[i]);
+            if (lane == 0 && i < segw) {
+                segmask[v * segw + i] = r;
+                segone[v * segw + i] = r1;
+            }
         }
     }
 }
@@ -934,11 +949,18 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                     const int t = oi < nv ? P.vlab[j] : -1;
                     if (t != cur_t) {
                         if (hits > 0) {
-                            const uint32_t segk = (uint32_t)(pack_entry(0, (uint32_t)cur_t, 0) >> 32);
-                            const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
-                            const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
-                            if (first && last && maxub - minlb == hits) {
-                                const uint32_t kc = (uint32_t)(cur_t - P.lbase);
+                            const uint32_t kc = (uint32_t)(cur_t - P.lbase);
+                            bool lost;
+                            if (hits == 1) {
+                                // One hit fills its segment only when the segment has one entry.
+                                lost = (__ldg(a.segone + (int64_t)u * mw + (kc >> 5)) >> (kc & 31u)) & 1u;
+                            } else {
+                                const uint32_t segk = (uint32_t)(pack_entry(0, (uint32_t)cur_t, 0) >> 32);
+                                const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
+                                const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
+                                lost = first && last && maxub - minlb == hits;
+                            }
+                            if (lost) {
 #pragma unroll
                                 for (int w = 0; w < kMaxMaskWords; ++w)
                                     ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
@@ -969,7 +991,9 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                     if (jj >= 0) {
                         const int32_t stored = __ldg(a.in_cols[a.ecol + jj] + row);
                         pos = P.e_from[jj] == vs ? stored : __ldg(a.rev + stored);
-                        if (pos < b || pos >= e || __ldg(a.adj + pos) != key) pos = -1;   // not where expected: search
+                        // The entry column holds the image edge's entry (or, from its
+                        // other end, the reverse entry): inside u's list it is the key.
+                        if (pos < b || pos >= e) pos = -1;
                     }
                     if (pos < 0) {
                         if (x == u && !((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
@@ -1417,7 +1441,7 @@ cudaError_t launch_segmask(DevGraph& g, cudaStream_t st)
 {
     if (g.n == 0 || g.segw == 0) return cudaSuccess;
     k_segmask<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.lwin, g.segw, g.vrank, g.win_base, g.offsets,
-                                                                 g.adj, g.segmask);
+                                                                 g.adj, g.segmask, g.segone);
     return cudaGetLastError();
 }
 
@@ -1428,6 +1452,7 @@ MaskDev mask_dev(const MaskArgs& x)
     a.offsets = x.g->offsets;
     a.adj = x.g->adj;
     a.segmask = x.g->segmask;
+    a.segone = x.g->segone;
     a.selfloop = x.g->selfloop;
     a.rev = x.g->rev;
     a.eidx = x.g->eidx;
