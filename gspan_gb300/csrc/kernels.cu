@@ -711,6 +711,8 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
 // reads, leaving both arrays zero for the next group of parents.
 
 constexpr int kMaskWarps = 8;
+// Pattern vertices whose mask words the row pass reads together (one word each).
+constexpr int kMaskBatch = 4;
 
 struct MaskDev {
     const int32_t* offsets;
@@ -1092,10 +1094,27 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
             for (int w = 0; w < kMaxMaskWords; ++w)
                 mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
             }
-            for (int p = 0; p < nv; ++p) {
-                uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * P.nloc + (live ? img[p] - P.vbase : 0)) * mw;
-                const int64_t out = P.sz_off + (int64_t)s * K * (nv + 1) + p;
-                for (int w = 0; w < mw; ++w) add_fresh_bits(or_fresh(rowm + w, mk[w]), a.sizes, out, nv + 1, w, lane);
+            if (mw == 1 && nv <= kMaskBatch) {
+                // One mask word per vertex: read every vertex's word first, so
+                // the L2 round trips overlap, then OR where bits are missing.
+                uint32_t* const mrow = a.M + P.m_off + (int64_t)s * (nv + 1) * P.nloc;
+                uint32_t cur[kMaskBatch];
+#pragma unroll
+                for (int p = 0; p < kMaskBatch; ++p)
+                    cur[p] = p < nv && mk[0] ? __ldcg(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase)) : ~0u;
+#pragma unroll
+                for (int p = 0; p < kMaskBatch; ++p) {
+                    if (p >= nv) break;
+                    const uint32_t fresh =
+                        (mk[0] & ~cur[p]) ? mk[0] & ~atomicOr(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase), mk[0]) : 0u;
+                    add_fresh_bits(fresh, a.sizes, P.sz_off + (int64_t)s * K * (nv + 1) + p, nv + 1, 0, lane);
+                }
+            } else {
+                for (int p = 0; p < nv; ++p) {
+                    uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * P.nloc + (live ? img[p] - P.vbase : 0)) * mw;
+                    const int64_t out = P.sz_off + (int64_t)s * K * (nv + 1) + p;
+                    for (int w = 0; w < mw; ++w) add_fresh_bits(or_fresh(rowm + w, mk[w]), a.sizes, out, nv + 1, w, lane);
+                }
             }
         }
 
