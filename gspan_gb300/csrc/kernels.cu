@@ -1265,7 +1265,7 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
         __syncwarp();
         if (lane == 0) *Ru = 0u;
     }
-    scanned += __shfl_xor_sync(kFull, scanned, 16);
+    // `scanned` is the same in every lane of the warp.
     if (lane == 0 && scanned) atomicAdd(a.scanned, scanned);
 }
 
