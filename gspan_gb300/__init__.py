@@ -56,7 +56,7 @@ class GspanError(RuntimeError):
 class Opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("domain_mode", ctypes.c_int32),
                 ("hash_threshold", ctypes.c_double), ("mem_fraction", ctypes.c_double),
-                ("profile", ctypes.c_int32), ("path", ctypes.c_int32)]
+                ("profile", ctypes.c_int32), ("path", ctypes.c_int32), ("mask_bias", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -133,6 +133,9 @@ _lib.gspan_server_submit.restype = ctypes.c_int
 _lib.gspan_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_int64, EMIT_FN, ctypes.c_void_p,
                                    ctypes.POINTER(JobInfo)]
 _lib.gspan_server_wait.restype = ctypes.c_int
+_lib.gspan_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Opts), ctypes.POINTER(ctypes.c_double)]
+_lib.gspan_autotune.restype = ctypes.c_int
 _lib.gspan_table_support.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]
 _lib.gspan_table_support.restype = ctypes.c_int
@@ -153,7 +156,7 @@ ABI_SYMBOLS = ("gspan_opts_default", "gspan_ctx_create", "gspan_ctx_destroy", "g
                "gspan_graph_free", "gspan_mine", "gspan_batch_upload", "gspan_mine_batch", "gspan_graph_instances",
                "gspan_table_support", "gspan_table_support_noalloc",
                "gspan_server_create", "gspan_server_destroy", "gspan_server_add_graph", "gspan_server_submit",
-               "gspan_server_wait", "gspan_is_canonical",
+               "gspan_server_wait", "gspan_autotune", "gspan_is_canonical",
                "gspan_status_string", "gspan_last_error", "gspan_max_pattern_edges")
 
 Code = tuple  # tuple of (from, to, from_label, edge_label, to_label)
@@ -189,7 +192,7 @@ class Miner:
     """One mining context on one GPU (a CUDA stream and the device memory it owns)."""
 
     def __init__(self, device: int = 0, domain_mode: int = 0, hash_threshold: float = 1.0,
-                 profile: bool = False, mem_fraction: float = 0.85, path: int = 0):
+                 profile: bool = False, mem_fraction: float = 0.85, path: int = 0, mask_bias: float = 1.0):
         opts = Opts()
         _lib.gspan_opts_default(ctypes.byref(opts))
         opts.device = device
@@ -198,6 +201,7 @@ class Miner:
         opts.profile = 1 if profile else 0
         opts.mem_fraction = mem_fraction
         opts.path = path
+        opts.mask_bias = mask_bias
         self._ctx = ctypes.c_void_p()
         rc = _lib.gspan_ctx_create(ctypes.byref(opts), ctypes.byref(self._ctx))
         if rc != GSPAN_OK:
@@ -291,6 +295,35 @@ class Miner:
         if rc != GSPAN_OK:
             raise self._err(rc, "gspan_mine_batch")
         return out, st.as_dict()
+
+    TUNABLES = ("domain_mode", "hash_threshold", "mem_fraction", "path", "mask_bias")
+
+    def autotune(self, dg: DeviceGraph, k: int, min_supports, candidates=None, ncand: int = 6, repeats: int = 2):
+        """Times the job under each option set (dicts of TUNABLES; None: the
+        built-in grid) and returns (the fastest set as Miner keyword arguments,
+        median milliseconds per set).  Every set must give identical results."""
+        ninst = int(_lib.gspan_graph_instances(dg.handle))
+        sups = np.ascontiguousarray(np.atleast_1d(min_supports), dtype=np.int32)
+        if sups.shape[0] != ninst:
+            raise ValueError("one min_support per instance")
+        cand_arr = None
+        if candidates is not None:
+            ncand = len(candidates)
+            cand_arr = (Opts * ncand)()
+            for o, c in zip(cand_arr, candidates):
+                _lib.gspan_opts_default(ctypes.byref(o))
+                for key, val in c.items():
+                    if key not in self.TUNABLES:
+                        raise ValueError(f"not a tunable: {key}")
+                    setattr(o, key, val)
+        best = Opts()
+        ms = (ctypes.c_double * max(ncand, 1))()
+        rc = _lib.gspan_autotune(self._ctx, dg.handle, int(k), sups.ctypes.data, cand_arr, int(ncand), int(repeats),
+                                 ctypes.byref(best), ms)
+        if rc != GSPAN_OK:
+            raise self._err(rc, "gspan_autotune")
+        n = ncand if candidates is not None else min(ncand, 6)
+        return {key: getattr(best, key) for key in self.TUNABLES}, list(ms)[:n]
 
     def table_support(self, cols, nr_nodes: int):
         """MNI support of an embedding table on the device (the reference's

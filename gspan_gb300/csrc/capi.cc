@@ -33,6 +33,7 @@ void gspan_opts_default(gspan_opts* o)
     o->mem_fraction = 0.85;
     o->profile = 0;
     o->path = 0;
+    o->mask_bias = 1.0;
 }
 
 const char* gspan_status_string(gspan_status s)

@@ -600,7 +600,8 @@ struct Run {
                 // rows x sources x (mean degree behind an embedding's vertex)
                 // candidates, each far dearer than clearing a word.
                 const double clear_words = (double)P.nsrc * (nv + 1) * P.nloc * g.segw + (double)nv * P.nloc * P.bw;
-                use_mask[i] = mode == 2 || (double)rows * P.nsrc * g.edge_biased_degree > 0.125 * clear_words;
+                const double bias = ctx->opts.mask_bias > 0 ? ctx->opts.mask_bias : 1.0;
+                use_mask[i] = mode == 2 || (double)rows * P.nsrc * g.edge_biased_degree > 0.125 * bias * clear_words;
             }
         }
 

@@ -62,6 +62,9 @@ typedef struct gspan_opts {
     int32_t profile;             /* 1: time every kernel launch with CUDA events into gspan_stats */
     int32_t path;                /* extension kernels: 0 auto, 1 per-candidate only, 2 mask path wherever the
                                     label space allows (both give identical results) */
+    double mask_bias;            /* auto path: a parent takes the mask path when its estimated candidate work
+                                    exceeds mask_bias / 8 x the dense words the mask path clears.
+                                    0 selects the default (1.0) */
 } gspan_opts;
 
 /* Run statistics.  Counts are exact and identical to those of the reference's
@@ -154,6 +157,18 @@ gspan_status gspan_mine_batch(gspan_ctx* ctx, const gspan_graph* batch, int32_t 
 
 /* Number of instances in an uploaded graph (1 for gspan_graph_upload). */
 int32_t gspan_graph_instances(const gspan_graph* graph);
+
+/* Autotuner: mines (graph, k, min_support) under each of `ncand` option sets
+ * (device and profile are taken from the context), one untimed run then
+ * `repeats` timed runs each, and checks that every set returns the same
+ * patterns and supports (GSPAN_ERR_DEVICE if not).  The fastest set goes to
+ * *best and each set's median wall time to ms[] (may be null).
+ * candidates == NULL uses the first min(ncand, 6) sets of a built-in grid
+ * over path, mask_bias and domain_mode.  min_support holds one threshold per instance
+ * (gspan_graph_instances).  No counterpart in the reference. */
+gspan_status gspan_autotune(gspan_ctx* ctx, const gspan_graph* graph, int32_t k, const int32_t* min_support,
+                            const gspan_opts* candidates, int32_t ncand, int32_t repeats, gspan_opts* best,
+                            double* ms);
 
 /* ---- Serving: requests accepted as they arrive, overlapping on the GPU ----
  * No counterpart in the reference (one graph per process run).  Graphs are
