@@ -133,6 +133,57 @@ _lib.gspan_server_submit.restype = ctypes.c_int
 _lib.gspan_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_int64, EMIT_FN, ctypes.c_void_p,
                                    ctypes.POINTER(JobInfo)]
 _lib.gspan_server_wait.restype = ctypes.c_int
+_lib.gspan_results_create.argtypes = []
+_lib.gspan_results_create.restype = ctypes.c_void_p
+_lib.gspan_results_destroy.argtypes = [ctypes.c_void_p]
+_lib.gspan_results_destroy.restype = None
+_lib.gspan_results_clear.argtypes = [ctypes.c_void_p]
+_lib.gspan_results_clear.restype = None
+_lib.gspan_results_patterns.argtypes = [ctypes.c_void_p]
+_lib.gspan_results_patterns.restype = ctypes.c_int64
+_lib.gspan_results_data.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+_lib.gspan_results_data.restype = ctypes.POINTER(ctypes.c_int32)
+# The collector's emit functions, passed to the miner as plain C pointers.
+_RESULTS_EMIT = ctypes.cast(_lib.gspan_results_emit, EMIT_FN)
+_RESULTS_BATCH_EMIT = ctypes.cast(_lib.gspan_results_batch_emit, BATCH_EMIT_FN)
+
+
+class _Collector:
+    """gspan_results: a run's patterns in one flat int32 buffer."""
+
+    def __init__(self):
+        self.h = _lib.gspan_results_create()
+        if not self.h:
+            raise MemoryError("gspan_results_create")
+
+    def array(self) -> np.ndarray:
+        n = ctypes.c_int64()
+        ptr = _lib.gspan_results_data(self.h, ctypes.byref(n))
+        if n.value == 0:
+            return np.zeros(0, dtype=np.int32)
+        return np.ctypeslib.as_array(ptr, shape=(n.value,)).copy()
+
+    def close(self):
+        if self.h:
+            _lib.gspan_results_destroy(self.h)
+            self.h = None
+
+
+def decode_results(flat: np.ndarray, ninst: int = 1) -> list:
+    """Flat collector words -> per instance [(code, support)], code a tuple
+    of (from, to, from_label, edge_label, to_label) tuples."""
+    out: list = [[] for _ in range(ninst)]
+    words = flat.tolist()
+    i, n = 0, len(words)
+    while i < n:
+        inst, length, sup = words[i], words[i + 1], words[i + 2]
+        j = i + 3
+        code = tuple(tuple(words[j + 5 * q: j + 5 * q + 5]) for q in range(length))
+        out[inst].append((code, sup))
+        i = j + 5 * length
+    return out
+
+
 _lib.gspan_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                 ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Opts), ctypes.POINTER(ctypes.c_double)]
 _lib.gspan_autotune.restype = ctypes.c_int
@@ -156,7 +207,9 @@ ABI_SYMBOLS = ("gspan_opts_default", "gspan_ctx_create", "gspan_ctx_destroy", "g
                "gspan_graph_free", "gspan_mine", "gspan_batch_upload", "gspan_mine_batch", "gspan_graph_instances",
                "gspan_table_support", "gspan_table_support_noalloc",
                "gspan_server_create", "gspan_server_destroy", "gspan_server_add_graph", "gspan_server_submit",
-               "gspan_server_wait", "gspan_autotune", "gspan_is_canonical",
+               "gspan_server_wait", "gspan_autotune", "gspan_results_create", "gspan_results_destroy",
+               "gspan_results_clear", "gspan_results_emit", "gspan_results_batch_emit", "gspan_results_patterns",
+               "gspan_results_data", "gspan_is_canonical",
                "gspan_status_string", "gspan_last_error", "gspan_max_pattern_edges")
 
 Code = tuple  # tuple of (from, to, from_label, edge_label, to_label)
@@ -241,22 +294,21 @@ class Miner:
             if rc != GSPAN_OK:
                 raise self._err(rc, "gspan_graph_free")
 
-    def mine(self, dg: DeviceGraph, k: int, min_support: int):
+    def mine(self, dg: DeviceGraph, k: int, min_support: int, raw: bool = False):
         """Returns (patterns, stats): patterns as [(code, support)] in the
-        reference's pre-order, code a tuple of 5-tuples."""
-        out: list = []
-
-        def emit(_user, code, length, support):
-            out.append((tuple((code[i].frm, code[i].to, code[i].from_label, code[i].edge_label,
-                               code[i].to_label) for i in range(length)), int(support)))
-            return 0
-
-        cb = EMIT_FN(emit)
-        st = Stats()
-        rc = _lib.gspan_mine(self._ctx, dg.handle, int(k), int(min_support), cb, None, ctypes.byref(st))
-        if rc != GSPAN_OK:
-            raise self._err(rc, "gspan_mine")
-        return out, st.as_dict()
+        reference's pre-order, code a tuple of 5-tuples; raw=True returns the
+        collector's flat int32 words instead (decode_results)."""
+        col = _Collector()
+        try:
+            st = Stats()
+            rc = _lib.gspan_mine(self._ctx, dg.handle, int(k), int(min_support), _RESULTS_EMIT, col.h,
+                                 ctypes.byref(st))
+            if rc != GSPAN_OK:
+                raise self._err(rc, "gspan_mine")
+            flat = col.array()
+        finally:
+            col.close()
+        return (flat if raw else decode_results(flat, 1)[0]), st.as_dict()
 
     def upload_batch(self, graphs) -> DeviceGraph:
         """Uploads many independent graphs as one batch (gspan_batch_upload)."""
@@ -276,25 +328,24 @@ class Miner:
         self._graphs.append(dg)
         return dg
 
-    def mine_batch(self, dg: DeviceGraph, k: int, min_supports):
-        """Returns (per-instance pattern lists, stats); each list as mine()."""
+    def mine_batch(self, dg: DeviceGraph, k: int, min_supports, raw: bool = False):
+        """Returns (per-instance pattern lists, stats); each list as mine().
+        raw=True returns the collector's flat words (decode_results)."""
         ninst = int(_lib.gspan_graph_instances(dg.handle))
-        out: list = [[] for _ in range(ninst)]
-
-        def emit(_user, inst, code, length, support):
-            out[inst].append((tuple((code[i].frm, code[i].to, code[i].from_label, code[i].edge_label,
-                                     code[i].to_label) for i in range(length)), int(support)))
-            return 0
-
-        cb = BATCH_EMIT_FN(emit)
         sups = np.ascontiguousarray(min_supports, dtype=np.int32)
         if sups.shape[0] != ninst:
             raise ValueError("one min_support per instance")
-        st = Stats()
-        rc = _lib.gspan_mine_batch(self._ctx, dg.handle, int(k), sups.ctypes.data, cb, None, ctypes.byref(st))
-        if rc != GSPAN_OK:
-            raise self._err(rc, "gspan_mine_batch")
-        return out, st.as_dict()
+        col = _Collector()
+        try:
+            st = Stats()
+            rc = _lib.gspan_mine_batch(self._ctx, dg.handle, int(k), sups.ctypes.data, _RESULTS_BATCH_EMIT, col.h,
+                                       ctypes.byref(st))
+            if rc != GSPAN_OK:
+                raise self._err(rc, "gspan_mine_batch")
+            flat = col.array()
+        finally:
+            col.close()
+        return (flat if raw else decode_results(flat, ninst)), st.as_dict()
 
     TUNABLES = ("domain_mode", "hash_threshold", "mem_fraction", "path", "mask_bias")
 
@@ -397,21 +448,18 @@ class Server:
 
     def wait(self, job_id: int):
         """Returns (patterns, info dict) of a finished job (blocks until done)."""
-        out: list = []
-
-        def emit(_user, code, length, support):
-            out.append((tuple((code[i].frm, code[i].to, code[i].from_label, code[i].edge_label,
-                               code[i].to_label) for i in range(length)), int(support)))
-            return 0
-
-        cb = EMIT_FN(emit)
-        info = JobInfo()
-        rc = _lib.gspan_server_wait(self._s, int(job_id), cb, None, ctypes.byref(info))
-        if rc != GSPAN_OK:
-            raise GspanError(rc, "gspan_server_wait")
+        col = _Collector()
+        try:
+            info = JobInfo()
+            rc = _lib.gspan_server_wait(self._s, int(job_id), _RESULTS_EMIT, col.h, ctypes.byref(info))
+            if rc != GSPAN_OK:
+                raise GspanError(rc, "gspan_server_wait")
+            flat = col.array()
+        finally:
+            col.close()
         d = {name: getattr(info, name) for name, _ in info._fields_ if name != "stats"}
         d["stats"] = info.stats.as_dict()
-        return out, d
+        return decode_results(flat, 1)[0], d
 
     def close(self) -> None:
         if self._s:

@@ -833,6 +833,31 @@ struct Run {
         dfree(d_MB, s);
         dfree(d_touched, s);
 
+        // Minimum-code tests the speculation did not reach, for children
+        // with enough embeddings: independent, so spread over the host cores.
+        {
+            std::vector<std::pair<int, int64_t>> need;
+            for (int i = 0; i < np; ++i) {
+                const int fl = parents[i].code[0].fl;
+                for (int64_t lk = 0; lk < key_span[i]; ++lk) {
+                    const size_t key = (size_t)(meta[i].key_base + lk);
+                    if (counts[key] != 0 && counts[key] >= threshold(fl) && canon[key] < 0) need.emplace_back(i, lk);
+                }
+            }
+            if (!need.empty()) {
+                const auto c0 = Clock::now();
+                const int64_t nn = (int64_t)need.size();
+#pragma omp parallel for schedule(dynamic, 16) if (nn > 64)
+                for (int64_t q = 0; q < nn; ++q) {
+                    std::vector<CodeEdge> child;
+                    const int i = need[(size_t)q].first;
+                    child_of(parents[i].code, meta[i], need[(size_t)q].second, child);
+                    canon[(size_t)(meta[i].key_base + need[(size_t)q].second)] =
+                        is_min_code(child.data(), (int)child.size()) ? 1 : 0;
+                }
+                st.canonical_ms += std::chrono::duration<double, std::milli>(Clock::now() - c0).count();
+            }
+        }
         // Which children count: enough embeddings, minimum code, and (mask
         // path) support from the domain sizes.
         std::vector<Freq> freq;
@@ -855,13 +880,7 @@ struct Run {
                                                   (lk - (int64_t)P.nsrc * K) * P.nv;
                 const int stride = 1;
                 ++st.canonical_checks;
-                int8_t cf = canon[(size_t)key];
-                if (cf < 0) {
-                    const auto c0 = Clock::now();
-                    cf = is_min_code(child.data(), (int)child.size()) ? 1 : 0;
-                    st.canonical_ms += std::chrono::duration<double, std::milli>(Clock::now() - c0).count();
-                }
-                if (!cf) continue;
+                if (!canon[(size_t)key]) continue;
                 if (use_mask[i]) {
                     uint32_t best = std::numeric_limits<uint32_t>::max();
                     for (int p = 0; p < nvc; ++p) {

@@ -158,6 +158,23 @@ gspan_status gspan_mine_batch(gspan_ctx* ctx, const gspan_graph* batch, int32_t 
 /* Number of instances in an uploaded graph (1 for gspan_graph_upload). */
 int32_t gspan_graph_instances(const gspan_graph* graph);
 
+/* Result collector: an emit target that appends every pattern to one flat
+ * int32 buffer, per pattern [instance, length, support, then length x (from,
+ * to, from_label, edge_label, to_label)], for callers that take all results
+ * at once instead of one callback per pattern.  Pass gspan_results_emit (or
+ * gspan_results_batch_emit) as the emit function and the collector as
+ * `user`.  Not thread-safe: one collector per concurrent mining call. */
+typedef struct gspan_results gspan_results;
+gspan_results* gspan_results_create(void);
+void gspan_results_destroy(gspan_results* results);
+void gspan_results_clear(gspan_results* results);
+int gspan_results_emit(void* results, const gspan_pattern_edge* code, int32_t len, int32_t support);
+int gspan_results_batch_emit(void* results, int32_t instance, const gspan_pattern_edge* code, int32_t len,
+                             int32_t support);
+int64_t gspan_results_patterns(const gspan_results* results);
+/* The buffer (valid until the next emit, clear or destroy) and its length in words. */
+const int32_t* gspan_results_data(const gspan_results* results, int64_t* nwords);
+
 /* Autotuner: mines (graph, k, min_support) under each of `ncand` option sets
  * (device and profile are taken from the context), one untimed run then
  * `repeats` timed runs each, and checks that every set returns the same
