@@ -184,6 +184,9 @@ def decode_results(flat: np.ndarray, ninst: int = 1) -> list:
     return out
 
 
+_lib.gspan_graph_upload_text.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p),
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+_lib.gspan_graph_upload_text.restype = ctypes.c_int
 _lib.gspan_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                 ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Opts), ctypes.POINTER(ctypes.c_double)]
 _lib.gspan_autotune.restype = ctypes.c_int
@@ -207,7 +210,7 @@ ABI_SYMBOLS = ("gspan_opts_default", "gspan_ctx_create", "gspan_ctx_destroy", "g
                "gspan_graph_free", "gspan_mine", "gspan_batch_upload", "gspan_mine_batch", "gspan_graph_instances",
                "gspan_table_support", "gspan_table_support_noalloc",
                "gspan_server_create", "gspan_server_destroy", "gspan_server_add_graph", "gspan_server_submit",
-               "gspan_server_wait", "gspan_autotune", "gspan_results_create", "gspan_results_destroy",
+               "gspan_server_wait", "gspan_autotune", "gspan_graph_upload_text", "gspan_results_create", "gspan_results_destroy",
                "gspan_results_clear", "gspan_results_emit", "gspan_results_batch_emit", "gspan_results_patterns",
                "gspan_results_data", "gspan_is_canonical",
                "gspan_status_string", "gspan_last_error", "gspan_max_pattern_edges")
@@ -284,6 +287,22 @@ class Miner:
         if rc != GSPAN_OK:
             raise self._err(rc, "gspan_graph_upload")
         dg = DeviceGraph(h, n, m)
+        self._graphs.append(dg)
+        return dg
+
+    def upload_text(self, text) -> DeviceGraph:
+        """Builds the device store from gSpan text (bytes or str, the
+        contents of a file that `convert` reads), parsed on the GPU."""
+        if isinstance(text, str):
+            text = text.encode()
+        buf = ctypes.create_string_buffer(bytes(text), len(text)) if text else None
+        h = ctypes.c_void_p()
+        n = ctypes.c_int32()
+        m = ctypes.c_int32()
+        rc = _lib.gspan_graph_upload_text(self._ctx, buf, len(text), ctypes.byref(h), ctypes.byref(n), ctypes.byref(m))
+        if rc != GSPAN_OK:
+            raise self._err(rc, "gspan_graph_upload_text")
+        dg = DeviceGraph(h, n.value, m.value)
         self._graphs.append(dg)
         return dg
 

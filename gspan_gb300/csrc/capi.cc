@@ -132,6 +132,19 @@ gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t n, int32_t m, const int3
     return gs::upload_graphs(ctx, 1, ns, ms, offs, vls, eds, out);
 }
 
+gspan_status gspan_graph_upload_text(gspan_ctx* ctx, const char* text, int64_t len, gspan_graph** out,
+                                     int32_t* nr_nodes, int32_t* nr_edges)
+{
+    if (!ctx || !out) return GSPAN_ERR_INVALID;
+    *out = nullptr;
+    ctx->err.clear();
+    try {
+        return gs::load_text(ctx, text, len, out, nr_nodes, nr_edges);
+    } catch (const std::bad_alloc&) {
+        return fail(ctx, GSPAN_ERR_NOMEM, "host allocation failed");
+    }
+}
+
 gspan_status gspan_batch_upload(gspan_ctx* ctx, int32_t ninst, const int32_t* nr_nodes, const int32_t* nr_edges,
                                 const int32_t* const* offsets, const int32_t* const* vlabels,
                                 const gspan_edge* const* edges, gspan_graph** out)

@@ -87,14 +87,38 @@ void free_graph(gspan_graph* gr, cudaStream_t st)
 
 
 gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, const int32_t* ms,
-                           const int32_t* const* offs, const int32_t* const* vls, const gspan_edge* const* eds,
-                           gspan_graph** out)
+                           const int32_t* const* offs_in, const int32_t* const* vls_in, const gspan_edge* const* eds_in,
+                           gspan_graph** out, bool on_device)
 {
+    // Device-resident input (one graph): the host reads only a copy of the
+    // offsets here, and of labels and edges for sparse label values below.
+    const int32_t* const* offs = offs_in;
+    const int32_t* const* vls = vls_in;
+    const gspan_edge* const* eds = eds_in;
+    std::vector<int32_t> h_off, h_vl;
+    std::vector<gspan_edge> h_ed;
+    const int32_t* h_offp[1] = {nullptr};
+    const int32_t* h_vlp[1] = {nullptr};
+    const gspan_edge* h_edp[1] = {nullptr};
+    const cudaMemcpyKind kin = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (on_device) {
+        if (ninst != 1 || ns[0] < 0 || ms[0] < 0 || !offs_in[0]) return fail(ctx, GSPAN_ERR_INVALID, "bad device graph");
+        cudaError_t e0 = cudaSetDevice(ctx->device);
+        if (e0 == cudaSuccess) {
+            h_off.resize((size_t)ns[0] + 1);
+            e0 = cudaMemcpyAsync(h_off.data(), offs_in[0], h_off.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        }
+        if (e0 == cudaSuccess) e0 = cudaStreamSynchronize(ctx->stream);
+        if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "read offsets");
+        h_offp[0] = h_off.data();
+        offs = h_offp;
+    }
     std::vector<int64_t> vbase((size_t)ninst + 1, 0), ebase((size_t)ninst + 1, 0);
     for (int32_t i = 0; i < ninst; ++i) {
         const int32_t n = ns[i], m = ms[i];
         if (n < 0 || m < 0) return fail(ctx, GSPAN_ERR_INVALID, "negative graph size");
-        if (!offs[i] || (n > 0 && !vls[i]) || (m > 0 && !eds[i])) return fail(ctx, GSPAN_ERR_INVALID, "null graph array");
+        if (!offs[i] || (n > 0 && !vls_in[i]) || (m > 0 && !eds_in[i]))
+            return fail(ctx, GSPAN_ERR_INVALID, "null graph array");
         if (offs[i][0] != 0 || offs[i][n] != m)
             return fail(ctx, GSPAN_ERR_INVALID, "offsets must start at 0 and end at nr_edges");
         vbase[(size_t)i + 1] = vbase[i] + n;
@@ -151,8 +175,7 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
             UP_CK(cudaMemcpyAsync(g.offsets + vbase[i], offs[i], (size_t)ns[i] * 4, cudaMemcpyHostToDevice, s),
                   "copy offsets");
         if (ms[i] > 0)
-            UP_CK(cudaMemcpyAsync(d_edges + ebase[i], eds[i], (size_t)ms[i] * sizeof(gspan_edge),
-                                  cudaMemcpyHostToDevice, s),
+            UP_CK(cudaMemcpyAsync(d_edges + ebase[i], eds[i], (size_t)ms[i] * sizeof(gspan_edge), kin, s),
                   "copy edges");
     }
     UP_CK(cudaMemcpyAsync(g.offsets + N, &M, 4, cudaMemcpyHostToDevice, s), "copy offsets");
@@ -175,7 +198,7 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
     const int32_t nv_dev = ninst == 1 ? N : 0;   // vertices ranked on the device
     if (nv_dev > 0) {
         UP_CK(cudaMallocAsync(&d_vl, (size_t)N * 4, s), "alloc labels");
-        UP_CK(cudaMemcpyAsync(d_vl, vls[0], (size_t)N * 4, cudaMemcpyHostToDevice, s), "copy labels");
+        UP_CK(cudaMemcpyAsync(d_vl, vls[0], (size_t)N * 4, kin, s), "copy labels");
     }
     UP_CK(cudaMallocAsync(&d_minmax, sizeof(mm), s), "alloc minmax");
     UP_CK(cudaMemcpyAsync(d_minmax, mm, sizeof(mm), cudaMemcpyHostToDevice, s), "init minmax");
@@ -219,6 +242,19 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         UP_CK(cudaStreamSynchronize(s), "rank tables");   // host tables leave scope
     } else {
         // Sparse label values: rank on the host.
+        if (on_device) {
+            h_vl.resize((size_t)N);
+            h_ed.resize((size_t)M);
+            if (N > 0) UP_CK(cudaMemcpyAsync(h_vl.data(), vls_in[0], (size_t)N * 4, cudaMemcpyDeviceToHost, s), "read labels");
+            if (M > 0)
+                UP_CK(cudaMemcpyAsync(h_ed.data(), eds_in[0], (size_t)M * sizeof(gspan_edge), cudaMemcpyDeviceToHost, s),
+                      "read edges");
+            UP_CK(cudaStreamSynchronize(s), "read labels");
+            h_vlp[0] = h_vl.data();
+            h_edp[0] = h_ed.data();
+            vls = h_vlp;
+            eds = h_edp;
+        }
         std::vector<int32_t> dist;
         for (int32_t i = 0; i < ninst; ++i) {
             if (ms[i] == 0) continue;

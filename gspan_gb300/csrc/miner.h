@@ -57,10 +57,14 @@ using EmitFn = std::function<int(int, const gspan_pattern_edge*, int32_t, int32_
 gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<int32_t>& minsup, const EmitFn& emit,
                   gspan_stats* stats);
 gspan_status fail(gspan_ctx* ctx, gspan_status s, const std::string& msg);
-// Builds the device store from `ninst` host CSR graphs (graph_store.cc).
+// Builds the device store from `ninst` CSR graphs (graph_store.cc): host
+// arrays, or (on_device, one graph) arrays already in device memory.
 gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, const int32_t* ms,
                            const int32_t* const* offs, const int32_t* const* vls, const gspan_edge* const* eds,
-                           gspan_graph** out);
+                           gspan_graph** out, bool on_device = false);
 void free_graph(gspan_graph* gr, cudaStream_t st);
+// Builds the device store from gSpan text read on the device (text_loader.cu).
+gspan_status load_text(gspan_ctx* ctx, const char* text, int64_t len, gspan_graph** out, int32_t* nr_nodes,
+                       int32_t* nr_edges);
 gspan_status cuda_fail(gspan_ctx* ctx, cudaError_t e, const char* what);
 }  // namespace gs

@@ -124,6 +124,20 @@ void gspan_ctx_destroy(gspan_ctx* ctx);
 gspan_status gspan_graph_upload(gspan_ctx* ctx, int32_t nr_nodes, int32_t nr_edges,
                                 const int32_t* offsets, const int32_t* vlabels,
                                 const gspan_edge* edges, gspan_graph** out);
+
+/* Device-side loader: builds the same device store from the bytes of a gSpan
+ * text file (the format convert.cc / graph.cc:38-64 read: 't # id', 'v id
+ * label', 'e from to label' records; other tokens skipped; the first integer
+ * that fails to parse ends the reading), parsed and turned into a CSR on the
+ * GPU.  Equivalent to reading the file with Graph::from_txt, building its
+ * CSRGraph and calling gspan_graph_upload.  Refuses (GSPAN_ERR_INVALID) the
+ * inputs a token-level parser cannot read like the reference's scanf-based
+ * reader: an integer directly followed by other characters, an integer
+ * outside int32, a token of 64 characters or more.  Vertex ids must span at
+ * most 2^28 values.  nr_nodes / nr_edges (may be null) receive the CSR's
+ * vertex and directed-entry counts. */
+gspan_status gspan_graph_upload_text(gspan_ctx* ctx, const char* text, int64_t len, gspan_graph** out,
+                                     int32_t* nr_nodes, int32_t* nr_edges);
 gspan_status gspan_graph_free(gspan_ctx* ctx, gspan_graph* graph);
 
 /* Mines every frequent pattern with at most `k` edges whose MNI support is
