@@ -48,3 +48,24 @@ def test_bad_requests():
         assert e.value.status == 1
         got, _ = srv.wait(srv.submit(gid, 2, 100))
         assert got
+
+
+def test_out_of_memory_job_among_others():
+    """A job too large for the device fails with NOMEM after its retry alone;
+    the jobs around it are unaffected."""
+    from gspan_gb300 import GspanError, Miner, Server, datagen
+    small = datagen.er_3300(0)
+    big = datagen.chung_lu_100k(1)
+    with Miner() as m:
+        want = m.fsm(small, 3, 20)[0]
+    with Server(slots=3) as srv:
+        gs_, gb = srv.add_graph(small), srv.add_graph(big)
+        hs = [srv.submit(gs_, 3, 20) for _ in range(3)]
+        hb = srv.submit(gb, 4, 1000)         # four-edge patterns at support 1,000: terabytes of embeddings
+        hs += [srv.submit(gs_, 3, 20) for _ in range(3)]
+        for h in hs:
+            got, info = srv.wait(h)
+            assert got == want and info["status"] == 0
+        with pytest.raises(GspanError) as e:
+            srv.wait(hb)
+        assert e.value.status == 3
