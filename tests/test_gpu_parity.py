@@ -145,3 +145,32 @@ def test_wide_label_space(miner):
     assert lines_of(patterns) == want
     assert got["extended"] == st["extended"]
     assert got["mask_parents"] == 0
+
+
+def test_fsm_cli_options():
+    """Optional flags after the reference's three arguments: kernel path,
+    domain representation, device-side text reading, JSON statistics."""
+    import json
+    from gspan_gb300 import datagen
+    case = [c for c in golden_cases() if c["name"] == "er3300" and c["min_support"] == 20][0]
+    g = golden_graph(case)
+    fsm = os.path.join(ROOT, "gspan_gb300", "_lib", "fsm")
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "g.bin")
+        g.save(path)
+        txt = os.path.join(tmp, "g.txt")
+        with open(txt, "w") as f:
+            f.write(datagen.to_gspan_text(g))
+        for args in (["--path", "candidate"], ["--path", "mask", "--domains", "bitmap"],
+                     ["--domains", "hash", "--stats"], ["--text", "--stats"]):
+            src = txt if "--text" in args else path
+            r = subprocess.run([fsm, src, "20", "3", *args], capture_output=True, text=True)
+            assert r.returncode == 0, (args, r.stderr)
+            out = r.stdout.splitlines()
+            assert out[-1].startswith("load:")
+            assert out[:-1] == golden_lines(case), args
+            if "--stats" in args:
+                st = json.loads(r.stderr.strip().splitlines()[-1])
+                assert st["patterns"] == len(out) - 1 and st["extended"] > 0
+        r = subprocess.run([fsm, path, "20", "3", "--path", "fast"], capture_output=True, text=True)
+        assert r.returncode == 1 and "--path" in r.stderr
