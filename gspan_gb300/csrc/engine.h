@@ -95,6 +95,11 @@ struct DevGraph {
     std::vector<int32_t> vlabel_of_rank, elabel_of_rank;
 };
 
+// Rows per tile of the Materialize pass (the other passes: 32, one per
+// lane).  Fewer rows give the tile queue more, lighter units to balance when
+// some rows' frequent segments are long (hubs).
+constexpr int kMatTileRows = 8;
+
 // Widest per-vertex key mask the mask kernels handle (x 32 keys).
 constexpr int kMaxMaskWords = 4;
 

@@ -491,8 +491,9 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
         const int nv = P.nv, nsrc = P.nsrc, nback = P.nback;
         const int32_t key_base = P.key_base;
         const int min_label = P.min_label;
-        const int64_t row = P.row_begin + (tile - P.tile_begin) * 32 + lane;
-        const bool live = row < P.row_end;
+        constexpr int kRows = kPass == Pass::Materialize ? kMatTileRows : 32;
+        const int64_t row = P.row_begin + (tile - P.tile_begin) * kRows + lane;
+        const bool live = lane < kRows && row < P.row_end;
 
         for (int p = 0; p < nv; ++p) Wimg[(lane) * a.vs + (p)] = live ? __ldcs(a.in_cols[p] + row) : -1;
 
@@ -673,7 +674,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                         for (int p = 0; p < nv; ++p) a.out_cols[p][r] = Wimg[(owner) * a.vs + (p)];
                         a.out_cols[nv][r] = (int32_t)to;
                         if (a.ecol_out >= 0) {
-                            const int64_t orow = P.row_begin + (tile - P.tile_begin) * 32 + owner;
+                            const int64_t orow = P.row_begin + (tile - P.tile_begin) * kRows + owner;
                             for (int jj = 0; jj < P.nedge; ++jj)
                                 a.out_cols[a.ecol_out + jj][r] = __ldg(a.in_cols[a.ecol_in + jj] + orow);
                             a.out_cols[a.ecol_out + P.nedge][r] = eidx;

@@ -627,7 +627,7 @@ struct Run {
             ParentMeta& A = all[i];
             const int64_t rows = A.row_end - A.row_begin;
             A.tile_begin = atiles;
-            atiles += (rows + 31) / 32;
+            atiles += (rows + kMatTileRows - 1) / kMatTileRows;
             all_read_bytes += (double)rows * (4.0 * A.nv + 8.0 * A.nsrc);
             if (!use_mask[i]) {
                 ParentMeta P = meta[i];
