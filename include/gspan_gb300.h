@@ -209,8 +209,9 @@ gspan_status gspan_autotune(gspan_ctx* ctx, const gspan_graph* graph, int32_t k,
  * first come, first served: the oldest waiting job starts when a slot is free
  * and its predicted working bytes fit `budget_bytes` (0: 60 % of the free
  * device memory) beside the running jobs; a job that runs out of device
- * memory beside others is re-run alone.  A server is driven by one host
- * thread (submit/wait); the workers are internal. */
+ * memory beside others is re-run alone.  add_graph, submit and wait may be
+ * called from any host threads (each job id is waited once); destroy only
+ * when no other call on the server is in progress. */
 typedef struct gspan_server gspan_server;
 
 typedef struct gspan_job_info {
@@ -224,7 +225,8 @@ typedef struct gspan_job_info {
 } gspan_job_info;
 
 gspan_status gspan_server_create(int32_t device, int32_t slots, double budget_bytes, gspan_server** out);
-/* Waits for the running jobs, then frees the graphs, contexts and server. */
+/* Lets the running jobs finish, drops the queued ones, then frees the
+ * graphs, contexts and server. */
 void gspan_server_destroy(gspan_server* server);
 gspan_status gspan_server_add_graph(gspan_server* server, int32_t nr_nodes, int32_t nr_edges, const int32_t* offsets,
                                     const int32_t* vlabels, const gspan_edge* edges, int32_t* graph_id);
