@@ -65,6 +65,11 @@ struct DevGraph {
     int32_t segw = 0;
     // Same layout: bit set when that segment holds exactly one entry.
     uint32_t* segone = nullptr;
+    // Per vertex, nel * lwin + 1 entry indices: where each (edge label, to
+    // label) key's segment starts in the adjacency (the lower bound of the
+    // key; the last one is the list's end).  Replaces the binary searches for
+    // range starts.  Built with segmask when it fits 4 GB, else null.
+    int32_t* segstart = nullptr;
     // Bit v set when vertex v has an entry to itself.
     uint32_t* selfloop = nullptr;
     // Every entry u->x with edge label l has a reverse entry x->u with label l
@@ -260,6 +265,7 @@ struct MaskArgs {
     uint32_t* status;
 };
 cudaError_t launch_segmask(DevGraph& g, cudaStream_t st);
+cudaError_t launch_segstart(DevGraph& g, cudaStream_t st);
 // Self-loop bitmap (zeroed by the caller) and the symmetry check: sets
 // kErrAsymmetric in *status when some entry has no reverse entry.
 cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st);

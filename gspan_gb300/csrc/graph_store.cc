@@ -69,6 +69,8 @@ void free_graph(gspan_graph* gr, cudaStream_t st)
     if (g.segmask) cudaFreeAsync(g.segmask, st);
     if (g.segone) cudaFreeAsync(g.segone, st);
     g.segone = nullptr;
+    if (g.segstart) cudaFreeAsync(g.segstart, st);
+    g.segstart = nullptr;
     if (g.selfloop) cudaFreeAsync(g.selfloop, st);
     if (g.rev) cudaFreeAsync(g.rev, st);
     g.rev = nullptr;
@@ -340,6 +342,11 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
             UP_CK(cudaMallocAsync(&g.segmask, (size_t)N * g.segw * 4, s), "alloc segment masks");
             UP_CK(cudaMallocAsync(&g.segone, (size_t)N * g.segw * 4, s), "alloc segment masks");
             UP_CK(launch_segmask(g, s), "segment mask launch");
+            const int64_t k1 = (int64_t)g.nel * g.lwin + 1;
+            if ((double)N * k1 * 4 <= 4.0 * (1u << 30)) {
+                UP_CK(cudaMallocAsync(&g.segstart, (size_t)N * k1 * 4, s), "alloc segment starts");
+                UP_CK(launch_segstart(g, s), "segment start launch");
+            }
         }
     }
     uint32_t status = 0;

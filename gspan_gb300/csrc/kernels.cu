@@ -440,6 +440,7 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
 struct ExpandDev {
     const int32_t* offsets;
     const uint64_t* adj;
+    const int32_t* segstart;     // segment starts per vertex (null: binary search)
     const uint64_t* eidx;        // edge index (null: binary search)
     uint32_t eidx_cap;
     int32_t nvl, nel, lwin;
@@ -509,15 +510,27 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                 const int sq = segs ? P.mseg_s[q] : q;
                 const int32_t u = Wimg[(lane) * a.vs + (P.src_v[sq])];
                 const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
+                const int32_t K1 = a.nel * a.lwin + 1;
                 if (segs) {
-                    const uint32_t el = P.mseg_kc[q] / (uint32_t)a.lwin;
-                    const uint32_t tl = (uint32_t)P.lbase + P.mseg_kc[q] % (uint32_t)a.lwin;
-                    st = lower_bound_entry(a.adj, b, e, pack_entry(el, tl, 0));
-                    c = lower_bound_entry(a.adj, st, e, pack_entry(el, tl + 1, 0)) - st;
+                    const uint32_t kc = P.mseg_kc[q];
+                    if (a.segstart) {
+                        st = __ldg(a.segstart + (int64_t)u * K1 + kc);
+                        c = __ldg(a.segstart + (int64_t)u * K1 + kc + 1) - st;
+                    } else {
+                        const uint32_t el = kc / (uint32_t)a.lwin;
+                        const uint32_t tl = (uint32_t)P.lbase + kc % (uint32_t)a.lwin;
+                        st = lower_bound_entry(a.adj, b, e, pack_entry(el, tl, 0));
+                        c = lower_bound_entry(a.adj, st, e, pack_entry(el, tl + 1, 0)) - st;
+                    }
                 } else {
-                    const uint64_t lo_key = sq == 0 ? pack_entry(0, (uint32_t)min_label, 0)
-                                                    : pack_entry((uint32_t)P.src_el[sq], (uint32_t)P.src_tl[sq], 0);
-                    st = lower_bound_entry(a.adj, b, e, lo_key);
+                    if (a.segstart) {
+                        const int32_t kc = sq == 0 ? min_label - P.lbase : P.src_el[sq] * a.lwin + P.src_tl[sq] - P.lbase;
+                        st = __ldg(a.segstart + (int64_t)u * K1 + kc);
+                    } else {
+                        const uint64_t lo_key = sq == 0 ? pack_entry(0, (uint32_t)min_label, 0)
+                                                        : pack_entry((uint32_t)P.src_el[sq], (uint32_t)P.src_tl[sq], 0);
+                        st = lower_bound_entry(a.adj, b, e, lo_key);
+                    }
                     c = e - st;
                 }
             }
@@ -720,6 +733,7 @@ struct MaskDev {
     const uint64_t* adj;
     const uint32_t* segmask;
     const uint32_t* segone;      // segments of exactly one entry
+    const int32_t* segstart;     // segment starts per vertex (null: binary search)
     const uint32_t* selfloop;
     const int32_t* rev;
     const uint64_t* eidx;        // edge index (null: binary search)
@@ -809,6 +823,39 @@ __global__ void k_segmask(int32_t n, int32_t lwin, int32_t segw, const int32_t* 
                 segone[v * segw + i] = r1;
             }
         }
+    }
+}
+
+// Warp per vertex: segstart[v][kc] = first entry of v whose window key is
+// >= kc, for kc in [0, K]; each kc is written once, by the entry that opens
+// it (or by the tail for keys after the last entry).
+__global__ void k_segstart(int32_t n, int32_t lwin, int32_t K, const int32_t* __restrict__ vrank,
+                           const int32_t* __restrict__ win_base, const int32_t* __restrict__ offsets,
+                           const uint64_t* __restrict__ adj, int32_t* __restrict__ segstart)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = warp; v < n; v += nwarps) {
+        const int32_t wb = win_base[vrank[v]];
+        const int32_t b = offsets[v], e = offsets[v + 1];
+        int32_t* out = segstart + v * (int64_t)(K + 1);
+        for (int32_t j = b + lane; j < e; j += 32) {
+            const uint64_t ent = adj[j];
+            const int32_t kc = (int32_t)(entry_el(ent) * (uint32_t)lwin + entry_tl(ent)) - wb;
+            int32_t kp = -1;
+            if (j > b) {
+                const uint64_t pe = adj[j - 1];
+                kp = (int32_t)(entry_el(pe) * (uint32_t)lwin + entry_tl(pe)) - wb;
+            }
+            for (int32_t k = kp + 1; k <= kc && k <= K; ++k) out[k] = j;
+        }
+        int32_t kl = -1;
+        if (e > b) {
+            const uint64_t le = adj[e - 1];
+            kl = (int32_t)(entry_el(le) * (uint32_t)lwin + entry_tl(le)) - wb;
+        }
+        for (int32_t k = kl + 1 + lane; k <= K; k += 32) out[k] = e;
     }
 }
 
@@ -1223,7 +1270,10 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
         const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
         const uint64_t lo_key = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
                                        : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
-        const int32_t st = lower_bound_entry(a.adj, b, e, lo_key);
+        const int32_t st = a.segstart ? __ldg(a.segstart + (int64_t)u * (a.nel * a.lwin + 1) +
+                                              (s == 0 ? min_label - P.lbase
+                                                      : P.src_el[s] * a.lwin + P.src_tl[s] - P.lbase))
+                                      : lower_bound_entry(a.adj, b, e, lo_key);
         uint32_t* Hs = a.H + P.h_off + (int64_t)s * P.mloc - P.ebase;
         uint32_t* NM = a.M + P.m_off + ((int64_t)s * (P.nv + 1) + P.nv) * P.nloc * mw;
         const int64_t nm_out = P.sz_off + (int64_t)s * K * (P.nv + 1) + P.nv;
@@ -1393,6 +1443,7 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     ExpandDev a;
     a.offsets = x.g->offsets;
     a.adj = x.g->adj;
+    a.segstart = x.g->segstart;
     a.eidx = x.g->eidx;
     a.eidx_cap = x.g->eidx_cap;
     a.nvl = x.g->nvl;
@@ -1457,6 +1508,14 @@ cudaError_t launch_edge_index(DevGraph& g, uint32_t* status, cudaStream_t st)
     return cudaGetLastError();
 }
 
+cudaError_t launch_segstart(DevGraph& g, cudaStream_t st)
+{
+    if (g.n == 0 || !g.segstart) return cudaSuccess;
+    k_segstart<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.lwin, g.nel * g.lwin, g.vrank,
+                                                                             g.win_base, g.offsets, g.adj, g.segstart);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_segmask(DevGraph& g, cudaStream_t st)
 {
     if (g.n == 0 || g.segw == 0) return cudaSuccess;
@@ -1473,6 +1532,7 @@ MaskDev mask_dev(const MaskArgs& x)
     a.adj = x.g->adj;
     a.segmask = x.g->segmask;
     a.segone = x.g->segone;
+    a.segstart = x.g->segstart;
     a.selfloop = x.g->selfloop;
     a.rev = x.g->rev;
     a.eidx = x.g->eidx;
