@@ -98,10 +98,11 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, settle_s: float = 0.3):
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.settle_s = settle_s
 
     def __enter__(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -112,7 +113,7 @@ class ClockSampler:
                  "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.proc = None
-        time.sleep(0.3)
+        time.sleep(self.settle_s)   # nvidia-smi's own start-up stays out of the timed steps
         return self
 
     def __exit__(self, *exc):
@@ -241,14 +242,16 @@ def gpu_arm(args, wl) -> None:
                          f"({r['extended']} extended embeddings in {r['fsm_s']:.3f} s); oracle port, OpenMP"}
 
     with Miner(device=local, profile=True) as m:
-        dg = m.upload_arrays(off_h, vl_h, ed_h)
-        for _ in range(args.warmup):
-            patterns, st = m.mine(dg, k, sup)
-        start = torch.cuda.Event(enable_timing=True)
-        end = torch.cuda.Event(enable_timing=True)
-        step_ms, stats = [], []
-        barrier()
-        with ClockSampler(local) as clk:
+        with ClockSampler(local, settle_s=1.0) as clk:
+            # The clock sampler starts before the warm-up, so its start-up does not
+            # land on a timed step; it samples through the timed region.
+            dg = m.upload_arrays(off_h, vl_h, ed_h)
+            for _ in range(args.warmup):
+                patterns, st = m.mine(dg, k, sup)
+            start = torch.cuda.Event(enable_timing=True)
+            end = torch.cuda.Event(enable_timing=True)
+            step_ms, stats = [], []
+            barrier()
             for _ in range(args.steps):
                 flush.zero_()
                 torch.cuda.synchronize(dev)

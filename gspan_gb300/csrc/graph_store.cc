@@ -333,22 +333,6 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
     }
     UP_CK(launch_build_adjacency(g.offsets, d_edges, d_etab, elo, d_elabels, g, d_tmp, ctx->d_status, s),
           "build adjacency launch");
-    // Per-vertex masks of the (edge label, to label) segments present, for the
-    // mask extension path; only when the window's tuple space fits the mask width.
-    {
-        const int64_t K = (int64_t)g.nel * g.lwin;
-        if (N > 0 && K > 0 && K <= 32 * kMaxMaskWords) {
-            g.segw = (int32_t)((K + 31) / 32);
-            UP_CK(cudaMallocAsync(&g.segmask, (size_t)N * g.segw * 4, s), "alloc segment masks");
-            UP_CK(cudaMallocAsync(&g.segone, (size_t)N * g.segw * 4, s), "alloc segment masks");
-            UP_CK(launch_segmask(g, s), "segment mask launch");
-            const int64_t k1 = (int64_t)g.nel * g.lwin + 1;
-            if ((double)N * k1 * 4 <= 4.0 * (1u << 30)) {
-                UP_CK(cudaMallocAsync(&g.segstart, (size_t)N * k1 * 4, s), "alloc segment starts");
-                UP_CK(launch_segstart(g, s), "segment start launch");
-            }
-        }
-    }
     uint32_t status = 0;
     UP_CK(cudaMemcpyAsync(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
     cleanup();
@@ -358,39 +342,52 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         return fail(ctx, GSPAN_ERR_INVALID, "malformed graph: offsets not monotone, an entry's `from` differs from "
                                             "its vertex, or a `to` is out of range");
     }
-    // Self-loop bits and the symmetry check, on the validated adjacency.
+    // On the validated adjacency, with one sync for all their flags:
+    // per-vertex segment masks and starts (for the mask extension path, when
+    // the window's tuple space fits the mask width), self-loop bits and the
+    // symmetry check, and the edge index (load factor in (3/8, 3/4]).
+    UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
+    {
+        const int64_t K = (int64_t)g.nel * g.lwin;
+        if (N > 0 && K > 0 && K <= 32 * kMaxMaskWords) {
+            g.segw = (int32_t)((K + 31) / 32);
+            UP_CK(cudaMallocAsync(&g.segmask, (size_t)N * g.segw * 4, s), "alloc segment masks");
+            UP_CK(cudaMallocAsync(&g.segone, (size_t)N * g.segw * 4, s), "alloc segment masks");
+            UP_CK(launch_segmask(g, s), "segment mask launch");
+            const int64_t k1 = K + 1;
+            if ((double)N * k1 * 4 <= 4.0 * (1u << 30)) {
+                UP_CK(cudaMallocAsync(&g.segstart, (size_t)N * k1 * 4, s), "alloc segment starts");
+                UP_CK(launch_segstart(g, s), "segment start launch");
+            }
+        }
+    }
     {
         const size_t words = ((size_t)N + 31) / 32 + 1;
-        uint32_t flags = 0;
         UP_CK(cudaMallocAsync(&g.selfloop, words * 4, s), "alloc self-loop bits");
         if (M > 0) UP_CK(cudaMallocAsync(&g.rev, (size_t)M * 4, s), "alloc reverse entries");
         UP_CK(cudaMemsetAsync(g.selfloop, 0, words * 4, s), "clear self-loop bits");
-        UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
         UP_CK(launch_graph_flags(g, ctx->d_status, s), "graph flags launch");
-        UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
-        UP_CK(cudaStreamSynchronize(s), "graph flags");
-        g.symmetric = !(flags & kErrAsymmetric);
-        g.loops = (flags & kFlagSelfLoop) != 0;
-        g.entry_cols = g.symmetric && g.nel == 1;
     }
-    // Edge index at a load factor in (3/8, 3/4].
-    g.parallel = true;
     if (M > 0 && M <= (1 << 30)) {
         uint32_t cap = 64;
         while ((uint64_t)cap < (uint64_t)M + M / 3) cap <<= 1;
-        uint32_t flags = 0;
         UP_CK(cudaMallocAsync(&g.eidx, (size_t)cap * 8, s), "alloc edge index");
         g.eidx_cap = cap;
         UP_CK(cudaMemsetAsync(g.eidx, 0xFF, (size_t)cap * 8, s), "clear edge index");
-        UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
         UP_CK(launch_edge_index(g, ctx->d_status, s), "edge index launch");
+    }
+    {
+        uint32_t flags = 0;
         UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
-        UP_CK(cudaStreamSynchronize(s), "edge index");
+        UP_CK(cudaStreamSynchronize(s), "graph flags");
         if (flags & kErrHashFull) {
             drop();
             return fail(ctx, GSPAN_ERR_CUDA, "edge index: a probe ran through the table");
         }
-        g.parallel = (flags & kFlagParallel) != 0;
+        g.symmetric = !(flags & kErrAsymmetric);
+        g.loops = (flags & kFlagSelfLoop) != 0;
+        g.entry_cols = g.symmetric && g.nel == 1;
+        g.parallel = !g.eidx || (flags & kFlagParallel) != 0;
     }
 #undef UP_CK
     ++ctx->live_graphs;

@@ -788,7 +788,7 @@ __device__ __forceinline__ void add_fresh_bits(uint32_t fresh, uint32_t* sizes, 
     if (mine) atomicAdd(sizes + out + (int64_t)(word * 32 + lane) * stride, mine);
 }
 
-__global__ void k_segmask(int32_t n, int32_t lwin, int32_t segw, const int32_t* __restrict__ vrank,
+__global__ void k_segmask(int32_t n, int32_t m, int32_t lwin, int32_t segw, const int32_t* __restrict__ vrank,
                           const int32_t* __restrict__ win_base, const int32_t* __restrict__ offsets,
                           const uint64_t* __restrict__ adj, uint32_t* __restrict__ segmask,
                           uint32_t* __restrict__ segone)
@@ -800,6 +800,7 @@ __global__ void k_segmask(int32_t n, int32_t lwin, int32_t segw, const int32_t* 
         uint32_t w[kMaxMaskWords] = {0, 0, 0, 0}, one[kMaxMaskWords] = {0, 0, 0, 0};
         const uint32_t wb = (uint32_t)win_base[vrank[v]];
         const int32_t b = offsets[v], e = offsets[v + 1];
+        if (b < 0 || e < b || e > m) continue;   // malformed range (rejected by the upload)
         for (int32_t j = b + lane; j < e; j += 32) {
             const uint64_t ent = adj[j];
             const uint32_t seg = (uint32_t)(ent >> 32);   // (edge label, to label)
@@ -829,7 +830,7 @@ __global__ void k_segmask(int32_t n, int32_t lwin, int32_t segw, const int32_t* 
 // Warp per vertex: segstart[v][kc] = first entry of v whose window key is
 // >= kc, for kc in [0, K]; each kc is written once, by the entry that opens
 // it (or by the tail for keys after the last entry).
-__global__ void k_segstart(int32_t n, int32_t lwin, int32_t K, const int32_t* __restrict__ vrank,
+__global__ void k_segstart(int32_t n, int32_t m, int32_t lwin, int32_t K, const int32_t* __restrict__ vrank,
                            const int32_t* __restrict__ win_base, const int32_t* __restrict__ offsets,
                            const uint64_t* __restrict__ adj, int32_t* __restrict__ segstart)
 {
@@ -839,6 +840,7 @@ __global__ void k_segstart(int32_t n, int32_t lwin, int32_t K, const int32_t* __
     for (int64_t v = warp; v < n; v += nwarps) {
         const int32_t wb = win_base[vrank[v]];
         const int32_t b = offsets[v], e = offsets[v + 1];
+        if (b < 0 || e < b || e > m) continue;   // malformed range (rejected by the upload)
         int32_t* out = segstart + v * (int64_t)(K + 1);
         for (int32_t j = b + lane; j < e; j += 32) {
             const uint64_t ent = adj[j];
@@ -1511,7 +1513,7 @@ cudaError_t launch_edge_index(DevGraph& g, uint32_t* status, cudaStream_t st)
 cudaError_t launch_segstart(DevGraph& g, cudaStream_t st)
 {
     if (g.n == 0 || !g.segstart) return cudaSuccess;
-    k_segstart<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.lwin, g.nel * g.lwin, g.vrank,
+    k_segstart<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, g.lwin, g.nel * g.lwin, g.vrank,
                                                                              g.win_base, g.offsets, g.adj, g.segstart);
     return cudaGetLastError();
 }
@@ -1519,7 +1521,7 @@ cudaError_t launch_segstart(DevGraph& g, cudaStream_t st)
 cudaError_t launch_segmask(DevGraph& g, cudaStream_t st)
 {
     if (g.n == 0 || g.segw == 0) return cudaSuccess;
-    k_segmask<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.lwin, g.segw, g.vrank, g.win_base, g.offsets,
+    k_segmask<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, g.lwin, g.segw, g.vrank, g.win_base, g.offsets,
                                                                  g.adj, g.segmask, g.segone);
     return cudaGetLastError();
 }
