@@ -106,7 +106,10 @@ struct DevGraph {
 constexpr int kMatTileRows = 8;
 
 // Widest per-vertex key mask the mask kernels handle (x 32 keys).
-constexpr int kMaxMaskWords = 4;
+constexpr int kMaxMaskWords = 16;
+// Mask words of the row pass's fast build (<= 128 tuple keys per label
+// window); wider label spaces use the kMaxMaskWords build.
+constexpr int kNarrowMaskWords = 4;
 
 // Where a domain (set of graph vertices that one pattern vertex maps to)
 // lives: `nvc` consecutive tables of `cap` 32-bit words starting at `off` in

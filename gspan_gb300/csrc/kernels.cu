@@ -797,7 +797,7 @@ __global__ void k_segmask(int32_t n, int32_t m, int32_t lwin, int32_t segw, cons
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t v = warp; v < n; v += nwarps) {
-        uint32_t w[kMaxMaskWords] = {0, 0, 0, 0}, one[kMaxMaskWords] = {0, 0, 0, 0};
+        uint32_t w[kMaxMaskWords] = {}, one[kMaxMaskWords] = {};
         const uint32_t wb = (uint32_t)win_base[vrank[v]];
         const int32_t b = offsets[v], e = offsets[v + 1];
         if (b < 0 || e < b || e > m) continue;   // malformed range (rejected by the upload)
@@ -932,7 +932,8 @@ __device__ __forceinline__ int32_t find_parent_tile(const ParentMeta* parents, i
 // Row pass: lane per row.  Updates R (listing new source images), H and M for
 // every source, and counts and MB masks for backward tuples (at most one per
 // row and rightmost-path target).
-__global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
+template <int MW>
+__global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 2) k_mask_rows(MaskDev a)
 {
     __shared__ int32_t img_s[kMaskWarps][32][kMaxV + 1];
     int32_t (*img_all)[kMaxV + 1] = img_s[threadIdx.x >> 5];
@@ -977,14 +978,14 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                         atomicOr(a.status, kErrCursor);
                 }
             }
-            uint32_t mk[kMaxMaskWords] = {0, 0, 0, 0};
+            uint32_t mk[MW] = {};
             if (live) {
             const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
             const uint64_t lo = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
                                        : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
             // H of this source, indexed by batch-wide entry index.
             uint32_t* Hs = a.H + P.h_off + (int64_t)s * P.mloc - P.ebase;
-            uint32_t ex[kMaxMaskWords] = {0, 0, 0, 0};
+            uint32_t ex[MW] = {};
             if (a.ecol >= 0) {
                 // One edge label.  Images joined to the source by a pattern
                 // edge are found through the row's entry columns (or their
@@ -1014,7 +1015,7 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                             }
                             if (lost) {
 #pragma unroll
-                                for (int w = 0; w < kMaxMaskWords; ++w)
+                                for (int w = 0; w < MW; ++w)
                                     ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
                             }
                         }
@@ -1134,14 +1135,14 @@ __global__ void __launch_bounds__(kMaskWarps * 32, 5) k_mask_rows(MaskDev a)
                         if (first && last && maxub - minlb == hits) {
                             const uint32_t kc = (uint32_t)(el * a.lwin + t - P.lbase);
 #pragma unroll
-                            for (int w = 0; w < kMaxMaskWords; ++w)
+                            for (int w = 0; w < MW; ++w)
                                 ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
                         }
                     }
                 }
             }
 #pragma unroll
-            for (int w = 0; w < kMaxMaskWords; ++w)
+            for (int w = 0; w < MW; ++w)
                 mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
             }
             if (mw == 1 && nv <= kMaskBatch) {
@@ -1584,7 +1585,11 @@ cudaError_t launch_mask_rows(const MaskArgs& x, cudaStream_t st)
     if (x.ntiles == 0) return cudaSuccess;
     const int64_t need = (x.ntiles + kMaskWarps - 1) / kMaskWarps;
     const int64_t cap = (int64_t)sm_count() * 8;
-    k_mask_rows<<<(int)(need < cap ? need : cap), kMaskWarps * 32, 0, st>>>(mask_dev(x));
+    const int grid = (int)(need < cap ? need : cap);
+    if (x.g->segw <= kNarrowMaskWords)
+        k_mask_rows<kNarrowMaskWords><<<grid, kMaskWarps * 32, 0, st>>>(mask_dev(x));
+    else
+        k_mask_rows<kMaxMaskWords><<<grid, kMaskWarps * 32, 0, st>>>(mask_dev(x));
     return cudaGetLastError();
 }
 

@@ -135,16 +135,29 @@ def test_unsorted_adjacency_input(miner):
 
 
 def test_wide_label_space(miner):
-    """150 vertex labels: the tuple space exceeds the mask width, so the upload
-    ranks entries without the counting sort and only the per-candidate kernels
-    run; the output still equals the oracle's."""
+    """150 vertex labels x 2 edge labels (300 tuple keys): the upload ranks
+    entries without the counting sort and the mask path uses its 16-word
+    build; the output equals the oracle's on every kernel path."""
     from gspan_gb300 import datagen
     g = datagen.erdos_renyi(3000, 9000, 150, 41, nelabels=2)
     want, st = run_port(g, 3, 3, threads=4, with_stats=True)
     patterns, got = miner.fsm(g, 3, 3)
     assert lines_of(patterns) == want
     assert got["extended"] == st["extended"]
-    assert got["mask_parents"] == 0
+
+
+def test_wide_label_space_paths():
+    """The mask path takes up to 512 tuple keys (16 mask words); beyond that
+    only the per-candidate kernels run."""
+    from gspan_gb300 import Miner, datagen
+    g300 = datagen.erdos_renyi(3000, 9000, 150, 41, nelabels=2)
+    g1k = datagen.erdos_renyi(4000, 12000, 330, 43, nelabels=3)
+    with Miner(path=2) as m:
+        p300, s300 = m.fsm(g300, 3, 3)
+        p1k, s1k = m.fsm(g1k, 3, 2)
+    assert s300["mask_parents"] > 0
+    assert s1k["mask_parents"] == 0
+    assert lines_of(p1k) == run_port(g1k, 2, 3, threads=4)
 
 
 def test_fsm_cli_options():
