@@ -187,3 +187,26 @@ def test_fsm_cli_options():
                 assert st["patterns"] == len(out) - 1 and st["extended"] > 0
         r = subprocess.run([fsm, path, "20", "3", "--path", "fast"], capture_output=True, text=True)
         assert r.returncode == 1 and "--path" in r.stderr
+
+
+def test_asymmetric_adjacency(miner):
+    """A CSR whose entries lack their reverse (the text reader never makes one,
+    but the C ABI accepts it): the symmetric shortcuts (entry columns, existence
+    tests from the shorter side) are off; the output still equals the port's."""
+    import numpy as np
+    from gspan_gb300 import datagen
+    rng = np.random.default_rng(11)
+    n, m = 400, 2400
+    u = rng.integers(0, n, m).astype(np.int32)
+    v = rng.integers(0, n, m).astype(np.int32)
+    el = rng.integers(0, 2, m).astype(np.int32)
+    order = np.lexsort((el, v, u))
+    u, v, el = u[order], v[order], el[order]
+    offsets = np.zeros(n + 1, dtype=np.int32)
+    np.add.at(offsets, u + 1, 1)
+    offsets = np.cumsum(offsets).astype(np.int32)
+    vlabels = rng.integers(0, 3, n).astype(np.int32)
+    g = datagen.CSR(offsets, vlabels, np.stack([u, v, el], axis=1).astype(np.int32))
+    want = run_port(g, 3, 3, threads=4)
+    patterns, st = miner.fsm(g, 3, 3)
+    assert lines_of(patterns) == want and len(want) > 0
