@@ -210,3 +210,19 @@ def test_asymmetric_adjacency(miner):
     want = run_port(g, 3, 3, threads=4)
     patterns, st = miner.fsm(g, 3, 3)
     assert lines_of(patterns) == want and len(want) > 0
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_deep_patterns(miner, seed):
+    """Patterns of 5 and 6 edges (up to 7 pattern vertices): the row pass's
+    general branches for more than 4 vertices, deep rightmost paths and many
+    backward targets; the output equals the port's."""
+    from gspan_gb300 import datagen
+    g = datagen.random_multigraph(9 + seed, 18 + 3 * seed, 1 + seed % 2, 1 + seed % 2, 700 + seed,
+                                  self_loops=seed % 3 == 0)
+    dg = miner.upload(g)
+    for sup, k in ((1, 5), (2, 6)):
+        patterns, st = miner.mine(dg, k, sup)
+        ref, ref_st = run_port(g, sup, k, threads=4, with_stats=True)
+        assert lines_of(patterns) == ref, (seed, sup, k)
+        assert st["extended"] == ref_st["extended"], (seed, sup, k)
