@@ -226,3 +226,16 @@ def test_deep_patterns(miner, seed):
         ref, ref_st = run_port(g, sup, k, threads=4, with_stats=True)
         assert lines_of(patterns) == ref, (seed, sup, k)
         assert st["extended"] == ref_st["extended"], (seed, sup, k)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_wide_mask_build_deep(seed):
+    """The row pass's 16-word build (129..512 tuple keys) at four edges, with
+    parallel edges and self-loops, forced onto the mask path."""
+    from gspan_gb300 import Miner, datagen
+    g = datagen.random_multigraph(160 + 20 * seed, 700 + 60 * seed, 60, 3, 800 + seed, self_loops=True)
+    ref, ref_st = run_port(g, 2, 4, threads=4, with_stats=True)
+    with Miner(path=2) as m:
+        patterns, st = m.fsm(g, 4, 2)
+    assert st["mask_parents"] > 0
+    assert lines_of(patterns) == ref and st["extended"] == ref_st["extended"]
