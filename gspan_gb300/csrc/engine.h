@@ -267,14 +267,14 @@ struct MaskArgs {
     unsigned long long* scanned; // adjacency entries read by the sweep
     uint32_t* status;
 };
-cudaError_t launch_segmask(DevGraph& g, cudaStream_t st);
-cudaError_t launch_segstart(DevGraph& g, cudaStream_t st);
-// Self-loop bitmap (zeroed by the caller) and the symmetry check: sets
-// kErrAsymmetric in *status when some entry has no reverse entry.
-cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st);
-// Fills g.eidx (all slots ~0 on entry); sets kFlagParallel in *status when a
-// vertex has two equal entries, kErrHashFull if a probe ran through the table.
-cudaError_t launch_edge_index(DevGraph& g, uint32_t* status, cudaStream_t st);
+// Segment masks (zeroed by the caller), singleton masks and, when
+// allocated, segment starts, in one pass over each vertex's entries.
+cudaError_t launch_segments(DevGraph& g, cudaStream_t st);
+// One pass over the entries: self-loop bitmap (zeroed by the caller), reverse
+// entries and the symmetry check (kErrAsymmetric), the edge index when
+// g.eidx is allocated (all slots ~0 on entry; kFlagParallel, kErrHashFull),
+// and kFlagSelfLoop.
+cudaError_t launch_entry_flags(DevGraph& g, uint32_t* status, cudaStream_t st);
 cudaError_t launch_mask_rows(const MaskArgs& a, cudaStream_t st);
 // Prefix of the touched lists, then the sweep (two launches).
 cudaError_t launch_mask_sweep(const MaskArgs& a, cudaStream_t st);

@@ -353,12 +353,12 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
             g.segw = (int32_t)((K + 31) / 32);
             UP_CK(cudaMallocAsync(&g.segmask, (size_t)N * g.segw * 4, s), "alloc segment masks");
             UP_CK(cudaMallocAsync(&g.segone, (size_t)N * g.segw * 4, s), "alloc segment masks");
-            UP_CK(launch_segmask(g, s), "segment mask launch");
+            UP_CK(cudaMemsetAsync(g.segmask, 0, (size_t)N * g.segw * 4, s), "clear segment masks");
+            UP_CK(cudaMemsetAsync(g.segone, 0, (size_t)N * g.segw * 4, s), "clear segment masks");
             const int64_t k1 = K + 1;
-            if ((double)N * k1 * 4 <= 4.0 * (1u << 30)) {
+            if ((double)N * k1 * 4 <= 4.0 * (1u << 30))
                 UP_CK(cudaMallocAsync(&g.segstart, (size_t)N * k1 * 4, s), "alloc segment starts");
-                UP_CK(launch_segstart(g, s), "segment start launch");
-            }
+            UP_CK(launch_segments(g, s), "segment launch");
         }
     }
     {
@@ -366,7 +366,6 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         UP_CK(cudaMallocAsync(&g.selfloop, words * 4, s), "alloc self-loop bits");
         if (M > 0) UP_CK(cudaMallocAsync(&g.rev, (size_t)M * 4, s), "alloc reverse entries");
         UP_CK(cudaMemsetAsync(g.selfloop, 0, words * 4, s), "clear self-loop bits");
-        UP_CK(launch_graph_flags(g, ctx->d_status, s), "graph flags launch");
     }
     if (M > 0 && M <= (1 << 30)) {
         uint32_t cap = 64;
@@ -374,8 +373,8 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         UP_CK(cudaMallocAsync(&g.eidx, (size_t)cap * 8, s), "alloc edge index");
         g.eidx_cap = cap;
         UP_CK(cudaMemsetAsync(g.eidx, 0xFF, (size_t)cap * 8, s), "clear edge index");
-        UP_CK(launch_edge_index(g, ctx->d_status, s), "edge index launch");
     }
+    UP_CK(launch_entry_flags(g, ctx->d_status, s), "entry flags launch");
     {
         uint32_t flags = 0;
         UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");

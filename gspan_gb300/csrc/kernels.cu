@@ -788,51 +788,17 @@ __device__ __forceinline__ void add_fresh_bits(uint32_t fresh, uint32_t* sizes, 
     if (mine) atomicAdd(sizes + out + (int64_t)(word * 32 + lane) * stride, mine);
 }
 
-__global__ void k_segmask(int32_t n, int32_t m, int32_t lwin, int32_t segw, const int32_t* __restrict__ vrank,
-                          const int32_t* __restrict__ win_base, const int32_t* __restrict__ offsets,
-                          const uint64_t* __restrict__ adj, uint32_t* __restrict__ segmask,
-                          uint32_t* __restrict__ segone)
-{
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t v = warp; v < n; v += nwarps) {
-        uint32_t w[kMaxMaskWords] = {}, one[kMaxMaskWords] = {};
-        const uint32_t wb = (uint32_t)win_base[vrank[v]];
-        const int32_t b = offsets[v], e = offsets[v + 1];
-        if (b < 0 || e < b || e > m) continue;   // malformed range (rejected by the upload)
-        for (int32_t j = b + lane; j < e; j += 32) {
-            const uint64_t ent = adj[j];
-            const uint32_t seg = (uint32_t)(ent >> 32);   // (edge label, to label)
-            const uint32_t kc = entry_el(ent) * (uint32_t)lwin + entry_tl(ent) - wb;
-            // Entries are sorted by segment: a singleton differs from both neighbours.
-            const bool single = (j == b || (uint32_t)(adj[j - 1] >> 32) != seg) &&
-                                (j + 1 == e || (uint32_t)(adj[j + 1] >> 32) != seg);
-#pragma unroll
-            for (int i = 0; i < kMaxMaskWords; ++i) {
-                const uint32_t bit = (uint32_t)(i == (int)(kc >> 5)) << (kc & 31u);
-                w[i] |= bit;
-                one[i] |= single ? bit : 0u;
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < kMaxMaskWords; ++i) {
-            const uint32_t r = __reduce_or_sync(kFull, w[i]);
-            const uint32_t r1 = __reduce_or_sync(kFull, one[i]);
-            if (lane == 0 && i < segw) {
-                segmask[v * segw + i] = r;
-                segone[v * segw + i] = r1;
-            }
-        }
-    }
-}
 
-// Warp per vertex: segstart[v][kc] = first entry of v whose window key is
-// >= kc, for kc in [0, K]; each kc is written once, by the entry that opens
-// it (or by the tail for keys after the last entry).
-__global__ void k_segstart(int32_t n, int32_t m, int32_t lwin, int32_t K, const int32_t* __restrict__ vrank,
-                           const int32_t* __restrict__ win_base, const int32_t* __restrict__ offsets,
-                           const uint64_t* __restrict__ adj, int32_t* __restrict__ segstart)
+// Warp per vertex, over its entries (sorted by window key kc): the entry
+// that opens segment kc sets bit kc of segmask, and of segone when it also
+// closes it; segstart[v][k] (when not null) = the first entry whose key is
+// >= k, for k in [0, K], each k written once (by the entry that opens it, or
+// by the tail for keys after the last entry).  segmask and segone start zero.
+__global__ void k_segments(int32_t n, int32_t m, int32_t lwin, int32_t K, int32_t segw,
+                           const int32_t* __restrict__ vrank, const int32_t* __restrict__ win_base,
+                           const int32_t* __restrict__ offsets, const uint64_t* __restrict__ adj,
+                           uint32_t* __restrict__ segmask, uint32_t* __restrict__ segone,
+                           int32_t* __restrict__ segstart)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -841,35 +807,55 @@ __global__ void k_segstart(int32_t n, int32_t m, int32_t lwin, int32_t K, const 
         const int32_t wb = win_base[vrank[v]];
         const int32_t b = offsets[v], e = offsets[v + 1];
         if (b < 0 || e < b || e > m) continue;   // malformed range (rejected by the upload)
-        int32_t* out = segstart + v * (int64_t)(K + 1);
+        auto key = [&](int32_t j) { return (int32_t)(entry_el(adj[j]) * (uint32_t)lwin + entry_tl(adj[j])) - wb; };
+        int32_t* out = segstart ? segstart + v * (int64_t)(K + 1) : nullptr;
         for (int32_t j = b + lane; j < e; j += 32) {
-            const uint64_t ent = adj[j];
-            const int32_t kc = (int32_t)(entry_el(ent) * (uint32_t)lwin + entry_tl(ent)) - wb;
-            int32_t kp = -1;
-            if (j > b) {
-                const uint64_t pe = adj[j - 1];
-                kp = (int32_t)(entry_el(pe) * (uint32_t)lwin + entry_tl(pe)) - wb;
+            const int32_t kc = key(j);
+            const int32_t kp = j > b ? key(j - 1) : -1;
+            if (kp < kc && kc >= 0 && kc < 32 * segw) {
+                const int64_t w = v * segw + (kc >> 5);
+                const uint32_t bit = 1u << (kc & 31);
+                atomicOr(segmask + w, bit);
+                if (j + 1 == e || key(j + 1) > kc) atomicOr(segone + w, bit);
             }
-            for (int32_t k = kp + 1; k <= kc && k <= K; ++k) out[k] = j;
+            if (out)
+                for (int32_t k = kp + 1; k <= kc && k <= K; ++k) out[k] = j;
         }
-        int32_t kl = -1;
-        if (e > b) {
-            const uint64_t le = adj[e - 1];
-            kl = (int32_t)(entry_el(le) * (uint32_t)lwin + entry_tl(le)) - wb;
+        if (out) {
+            const int32_t kl = e > b ? key(e - 1) : -1;
+            for (int32_t k = kl + 1 + lane; k <= K; k += 32) out[k] = e;
         }
-        for (int32_t k = kl + 1 + lane; k <= K; k += 32) out[k] = e;
     }
 }
 
-// Thread per entry: self-loop bits, and whether the entry's reverse exists.
-__global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const int32_t* __restrict__ offsets,
+
+// Thread per entry: self-loop bits, the entry's reverse entry (the k-th of
+// a run of equal entries pairs with the k-th of the reverse run) and the
+// symmetry check; and the edge index: the first entry of each run of equal
+// entries is inserted (linear probing, bounded by the table size).
+__global__ void k_entry_flags(int32_t m, const int32_t* __restrict__ src, const int32_t* __restrict__ offsets,
                               const uint64_t* __restrict__ adj, const int32_t* __restrict__ vrank,
-                              uint32_t* __restrict__ selfloop, int32_t* __restrict__ rev, uint32_t* status)
+                              uint32_t* __restrict__ selfloop, int32_t* __restrict__ rev,
+                              unsigned long long* __restrict__ eidx, uint32_t cap, uint32_t* status)
 {
-    bool asym = false, loop = false;
+    bool asym = false, loop = false, parallel = false, full = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t ent = adj[i];
         const uint32_t u = (uint32_t)src[i], x = entry_to(ent);
+        const int32_t bu = offsets[u];
+        const bool repeat = i > bu && adj[i - 1] == ent;
+        parallel |= repeat;
+        if (eidx && !repeat) {
+            const uint64_t h = edge_hash(u, entry_el(ent), x);
+            const unsigned long long val = ((h >> 32) << 32) | (uint32_t)i;
+            uint32_t j = (uint32_t)h & (cap - 1);
+            uint32_t probe = 0;
+            for (; probe < cap; ++probe) {
+                if (atomicCAS(eidx + j, ~0ull, val) == ~0ull) break;
+                j = (j + 1) & (cap - 1);
+            }
+            full |= probe == cap;
+        }
         if (u == x) {
             atomicOr(selfloop + (u >> 5), 1u << (u & 31));
             rev[i] = (int32_t)i;
@@ -878,7 +864,6 @@ __global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const 
         }
         // Rank of i among the equal entries before it (parallel edges with one label).
         int32_t r0 = (int32_t)i;
-        const int32_t bu = offsets[u];
         while (r0 > bu && adj[r0 - 1] == ent) --r0;
         const uint64_t rk = pack_entry(entry_el(ent), (uint32_t)vrank[u], u);
         const int32_t b = offsets[x], e = offsets[x + 1];
@@ -888,35 +873,10 @@ __global__ void k_graph_flags(int32_t m, const int32_t* __restrict__ src, const 
         asym |= !found;
     }
     const unsigned am = __ballot_sync(kFull, asym), lm = __ballot_sync(kFull, loop);
-    if ((threadIdx.x & 31) == 0 && (am | lm)) atomicOr(status, (am ? kErrAsymmetric : 0u) | (lm ? kFlagSelfLoop : 0u));
-}
-
-// Thread per entry: the first entry of each run of equal entries goes into
-// the edge index (linear probing, bounded by the table size).
-__global__ void k_edge_index(int32_t m, const int32_t* __restrict__ src, const int32_t* __restrict__ offsets,
-                             const uint64_t* __restrict__ adj, unsigned long long* __restrict__ eidx, uint32_t cap,
-                             uint32_t* status)
-{
-    bool parallel = false, full = false;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t ent = adj[i];
-        const int32_t u = src[i];
-        if (i > offsets[u] && adj[i - 1] == ent) {
-            parallel = true;
-            continue;
-        }
-        const uint64_t h = edge_hash((uint32_t)u, entry_el(ent), entry_to(ent));
-        const unsigned long long val = ((h >> 32) << 32) | (uint32_t)i;
-        uint32_t j = (uint32_t)h & (cap - 1);
-        uint32_t probe = 0;
-        for (; probe < cap; ++probe) {
-            if (atomicCAS(eidx + j, ~0ull, val) == ~0ull) break;
-            j = (j + 1) & (cap - 1);
-        }
-        full |= probe == cap;
-    }
     const unsigned pm = __ballot_sync(kFull, parallel), fm = __ballot_sync(kFull, full);
-    if ((threadIdx.x & 31) == 0 && (pm | fm)) atomicOr(status, (pm ? kFlagParallel : 0u) | (fm ? kErrHashFull : 0u));
+    if ((threadIdx.x & 31) == 0 && (am | lm | pm | fm))
+        atomicOr(status, (am ? kErrAsymmetric : 0u) | (lm ? kFlagSelfLoop : 0u) | (pm ? kFlagParallel : 0u) |
+                             (fm ? kErrHashFull : 0u));
 }
 
 __device__ __forceinline__ int32_t find_parent_tile(const ParentMeta* parents, int32_t np, long long tile)
@@ -1495,35 +1455,23 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t launch_graph_flags(DevGraph& g, uint32_t* status, cudaStream_t st)
+cudaError_t launch_entry_flags(DevGraph& g, uint32_t* status, cudaStream_t st)
 {
     if (g.m == 0) return cudaSuccess;
-    k_graph_flags<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj, g.vrank, g.selfloop, g.rev,
+    k_entry_flags<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj, g.vrank, g.selfloop, g.rev,
+                                                      reinterpret_cast<unsigned long long*>(g.eidx), g.eidx_cap,
                                                       status);
     return cudaGetLastError();
 }
 
-cudaError_t launch_edge_index(DevGraph& g, uint32_t* status, cudaStream_t st)
-{
-    if (g.m == 0 || !g.eidx) return cudaSuccess;
-    k_edge_index<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj,
-                                                     reinterpret_cast<unsigned long long*>(g.eidx), g.eidx_cap, status);
-    return cudaGetLastError();
-}
 
-cudaError_t launch_segstart(DevGraph& g, cudaStream_t st)
-{
-    if (g.n == 0 || !g.segstart) return cudaSuccess;
-    k_segstart<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, g.lwin, g.nel * g.lwin, g.vrank,
-                                                                             g.win_base, g.offsets, g.adj, g.segstart);
-    return cudaGetLastError();
-}
 
-cudaError_t launch_segmask(DevGraph& g, cudaStream_t st)
+cudaError_t launch_segments(DevGraph& g, cudaStream_t st)
 {
     if (g.n == 0 || g.segw == 0) return cudaSuccess;
-    k_segmask<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, g.lwin, g.segw, g.vrank, g.win_base, g.offsets,
-                                                                 g.adj, g.segmask, g.segone);
+    k_segments<<<grid_for((int64_t)g.n * 32, 256), 256, 0, st>>>(g.n, g.m, g.lwin, g.nel * g.lwin, g.segw, g.vrank,
+                                                                 g.win_base, g.offsets, g.adj, g.segmask, g.segone,
+                                                                 g.segstart);
     return cudaGetLastError();
 }
 
