@@ -80,6 +80,7 @@ void worker(gspan_server* s, gspan_ctx* ctx)
 {
     for (;;) {
         Job* job = nullptr;
+        const gspan_graph* graph = nullptr;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv_work.wait(lk, [&] { return s->stop || (!s->queue.empty() && admissible(s, s->queue.front())); });
@@ -89,6 +90,7 @@ void worker(gspan_server* s, gspan_ctx* ctx)
             ++s->running;
             s->in_use += job->predicted;
             job->started = Clock::now();
+            graph = s->graphs[job->graph];   // under the lock: add_graph may grow the vector
         }
         job->codes.clear();
         job->supports.clear();
@@ -99,7 +101,7 @@ void worker(gspan_server* s, gspan_ctx* ctx)
             jb->supports.push_back(sup);
             return 0;
         };
-        const gspan_status rc = gspan_mine(ctx, s->graphs[job->graph], job->k, job->min_support, collect, job, &st);
+        const gspan_status rc = gspan_mine(ctx, graph, job->k, job->min_support, collect, job, &st);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             --s->running;
