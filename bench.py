@@ -24,6 +24,10 @@ cpu_baseline = the CPU oracle port (the reference's algorithm, OpenMP on all
 resident graphs of the three single-graph sizes; jobs/s with p50/p95/p99
 latency, each result checked against the same job run alone.
 --workload batch_256: the batched engine against the plain one.
+--workload chung_lu_3_7m / chung_lu_3_7m_k4 / chung_lu_100k_wide: other
+single-graph jobs (the large graph at 3 and 4 edges; a wide label space).
+--workload text_load: loading a graph from gSpan text on the device against
+the host reader and upload.
 
 --impl reference times that CPU implementation alone (rank 0; other ranks
 exit) and prints the same line with "impl": "reference".
@@ -67,6 +71,18 @@ def workloads():
             make=lambda: datagen.chung_lu_3_7m(3), min_support=20000, k=3, sample_k=None,
             desc="Chung-Lu 3,700,000 V / 16,500,000 E, exponent 2.3, degree cap sqrt(2m), 37 vertex labels "
                  "Zipf(0.8), 1 edge label, seed 3"),
+        # The large graph at four edges, at the highest support range where its
+        # level-3 embedding table fits the device (about 8.6e9 rows).
+        "chung_lu_3_7m_k4": dict(
+            make=lambda: datagen.chung_lu_3_7m(3), min_support=100000, k=4, sample_k=None,
+            desc="Chung-Lu 3,700,000 V / 16,500,000 E (as chung_lu_3_7m), min support 100,000, 4 edges"),
+        # A wide label space: 100 vertex labels x 3 edge labels = 300 tuple keys
+        # (the row pass's 16-word build).
+        "chung_lu_100k_wide": dict(
+            make=lambda: datagen.chung_lu(100_000, 1_080_000, 2.1, 100, 1.0, 5, max_deg=1400, nelabels=3),
+            min_support=3000, k=3, sample_k=2,
+            desc="Chung-Lu 100,000 V / 1,080,000 E, exponent 2.1, degree cap 1,400, 100 vertex labels Zipf(1.0), "
+                 "3 edge labels, seed 5"),
         "er_3300": dict(
             make=lambda: datagen.er_3300(0), min_support=20, k=3, sample_k=3,
             desc="Erdos-Renyi 3,300 V / 4,700 E, 6 uniform vertex labels, 1 edge label, seed 0"),
@@ -488,6 +504,41 @@ def serving_arm(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def text_arm(args) -> None:
+    """Loading a graph from gSpan text: on the device (gspan_graph_upload_text:
+    tokens to device store on the GPU) against the host path (the convert tool's
+    reader and CSR build, writing and reading the .bin, then the upload)."""
+    from gspan_gb300 import Miner, datagen
+    g = datagen.chung_lu_100k(1)
+    text = datagen.to_gspan_text(g).encode()
+    convert = os.path.join(ROOT, "gspan_gb300", "_lib", "convert")
+    dev_ms, host_ms = [], []
+    with Miner() as m, tempfile.TemporaryDirectory() as tmp:
+        src, dst = os.path.join(tmp, "g.txt"), os.path.join(tmp, "g.bin")
+        with open(src, "wb") as f:
+            f.write(text)
+        for step in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            dg = m.upload_text(text)
+            d = time.perf_counter() - t
+            m.free(dg)
+            t = time.perf_counter()
+            subprocess.run([convert, src, dst], check=True, capture_output=True)
+            dg = m.upload(datagen.load_bin(dst))
+            h = time.perf_counter() - t
+            m.free(dg)
+            if step >= args.warmup:
+                dev_ms.append(1e3 * d)
+                host_ms.append(1e3 * h)
+    print(json.dumps({
+        "metric": "graph load from gSpan text (device loader vs host reader + upload)",
+        "value": statistics.median(dev_ms), "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "data": "synthetic (seeded generator)",
+        "config": {"workload": "text_load", "description": "chung_lu_100k as gSpan text",
+                   "text_bytes": len(text)},
+        "host_ms": statistics.median(host_ms)}), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -502,6 +553,9 @@ def main() -> None:
     args = ap.parse_args()
     if args.workload == "serving":
         serving_arm(args)
+        return
+    if args.workload == "text_load":
+        text_arm(args)
         return
     if args.workload in ("batch_256", "batch_16"):
         batch_arm(args)
