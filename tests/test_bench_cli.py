@@ -1,0 +1,36 @@
+"""bench.py on the CPU: the workload list, and the reference arm (the CPU
+implementation of the path), which needs no GPU."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run_bench(*args):
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], capture_output=True, text=True,
+                       timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def test_workloads_listed():
+    sys.path.insert(0, ROOT)
+    import bench
+    names = set(bench.workloads())
+    assert {"chung_lu_100k", "chung_lu_100k_s15k", "chung_lu_3_7m", "chung_lu_3_7m_k4", "chung_lu_100k_wide",
+            "er_3300"} <= names
+
+
+def test_reference_arm_line():
+    line = run_bench("--impl", "reference", "--workload", "er_3300", "--steps", "1", "--warmup", "0")
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "embeddings/s"
+    assert line["higher_is_better"] is True and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["extended_per_step"] > 0
+
+
+def test_reference_arm_unavailable_where_the_port_cannot_run():
+    line = run_bench("--impl", "reference", "--workload", "chung_lu_3_7m")
+    assert line["impl"] == "reference" and "unavailable" in line
