@@ -9,16 +9,27 @@ edges and its exact MNI support - over one seeded synthetic graph:
                     labels Zipf(1.0), 1 edge label, seed 1; min support
                     10,000; patterns up to 3 edges.
 
-value  = extended embeddings per second with the graph already resident in
-         HBM (child embeddings produced by extending frequent patterns; the
-         same count the reference's CPU path produces for this job).
-e2e    = the same metric through the C ABI from pinned host buffers: graph
-         upload (host->device, adjacency build), mining, results back to host.
-roofline = the extension kernel: algorithmic bytes / CUDA-event time, against
+value  = mining time per job in milliseconds (lower is better), graph already
+         resident in HBM, results delivered to host memory.
+e2e    = the same through the C ABI from pinned host buffers: graph upload
+         (host->device, adjacency build), mining, results back to host.
+embeddings_per_s = extended embeddings per second: child embeddings of
+         frequent patterns, the count the reference's extension produces.  The
+         GPU's mask path counts most of them without enumerating them one by
+         one, so this is a rate of the job, not of per-child work.
+roofline = the dominant kernel: algorithmic bytes / CUDA-event time, against
          the measured HBM copy bandwidth.
 cpu_baseline = the CPU oracle port (the reference's algorithm, OpenMP on all
-         host cores) on a bounded sample of the same workload: the same graph
-         and threshold at 2 edges.
+         host cores, last level counted without storing it) on a bounded
+         sample of the same job: everything above the last level plus one
+         slice of the last level's parent embeddings, scaled to a whole job.
+
+--impl reference times that CPU implementation on the same job (rank 0; other
+ranks exit): step i runs the levels above the last plus slice i of K of the
+last level's parent embeddings, so the K timed steps together cover the whole
+last level once; value = median time above the last level + the sum of the
+slices' last-level times.  The slices' extended-embedding counts are checked
+to add up to the whole job's.
 
 --workload serving: a Poisson stream (mean --rate jobs/s) of jobs over
 resident graphs of the three single-graph sizes; jobs/s with p50/p95/p99
@@ -29,11 +40,8 @@ single-graph jobs (the large graph at 3 and 4 edges; a wide label space).
 --workload text_load: loading a graph from gSpan text on the device against
 the host reader and upload.
 
---impl reference times that CPU implementation alone (rank 0; other ranks
-exit) and prints the same line with "impl": "reference".
-
 Multi-GPU (torchrun, N > 1): replicas only - every rank mines the same job on
-its own GPU; value = jobs' embeddings on all ranks / slowest rank's time.
+its own GPU; value = slowest rank's time / jobs on all ranks.
 """
 from __future__ import annotations
 
@@ -50,41 +58,56 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "mining time & embeddings/s, batched vs plain on 1 GB300 (exact patterns+MNI)"
-UNIT = "embeddings/s"
+UNIT = "ms/job"
+EMB_UNIT = "embeddings/s"
+
+
+def load_datagen():
+    """The seeded generators, loaded as a plain module: the reference arm must
+    not map this repository's native library (the package's top level loads it
+    on first use of a native name, and datagen needs none)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gspan_gb300_datagen",
+                                                  os.path.join(ROOT, "gspan_gb300", "datagen.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
 
 
 def workloads():
-    from gspan_gb300 import datagen
+    """Single-graph jobs.  cpu: whether the streaming CPU port finishes the whole
+    job within minutes on a 16-core host (the 3.7M-vertex jobs take hours)."""
+    datagen = load_datagen()
     return {
         "chung_lu_100k": dict(
-            make=lambda: datagen.chung_lu_100k(1), min_support=10000, k=3, sample_k=2,
+            make=lambda: datagen.chung_lu_100k(1), min_support=10000, k=3, cpu=True,
             desc="Chung-Lu 100,000 V / 1,080,000 E, exponent 2.1, degree cap 1,400, 29 vertex labels Zipf(1.0), "
                  "1 edge label, seed 1"),
         # Smaller case of the same kernels for profiler captures: the same graph
         # at a threshold that leaves one frequent 2-edge pattern to extend.
         "chung_lu_100k_s15k": dict(
-            make=lambda: datagen.chung_lu_100k(1), min_support=15000, k=3, sample_k=2,
+            make=lambda: datagen.chung_lu_100k(1), min_support=15000, k=3, cpu=True,
             desc="Chung-Lu 100,000 V / 1,080,000 E (as chung_lu_100k), min support 15,000"),
         # The large single graph, at 3 edges: its 4-edge level needs a level-3
         # embedding table of about 1.1e12 rows, beyond the device.
         "chung_lu_3_7m": dict(
-            make=lambda: datagen.chung_lu_3_7m(3), min_support=20000, k=3, sample_k=None,
+            make=lambda: datagen.chung_lu_3_7m(3), min_support=20000, k=3, cpu=False,
             desc="Chung-Lu 3,700,000 V / 16,500,000 E, exponent 2.3, degree cap sqrt(2m), 37 vertex labels "
                  "Zipf(0.8), 1 edge label, seed 3"),
         # The large graph at four edges, at the highest support range where its
         # level-3 embedding table fits the device (about 8.6e9 rows).
         "chung_lu_3_7m_k4": dict(
-            make=lambda: datagen.chung_lu_3_7m(3), min_support=100000, k=4, sample_k=None,
+            make=lambda: datagen.chung_lu_3_7m(3), min_support=100000, k=4, cpu=False,
             desc="Chung-Lu 3,700,000 V / 16,500,000 E (as chung_lu_3_7m), min support 100,000, 4 edges"),
         # A wide label space: 100 vertex labels x 3 edge labels = 300 tuple keys
         # (the row pass's 16-word build).
         "chung_lu_100k_wide": dict(
             make=lambda: datagen.chung_lu(100_000, 1_080_000, 2.1, 100, 1.0, 5, max_deg=1400, nelabels=3),
-            min_support=3000, k=3, sample_k=2,
+            min_support=3000, k=3, cpu=True,
             desc="Chung-Lu 100,000 V / 1,080,000 E, exponent 2.1, degree cap 1,400, 100 vertex labels Zipf(1.0), "
                  "3 edge labels, seed 5"),
         "er_3300": dict(
-            make=lambda: datagen.er_3300(0), min_support=20, k=3, sample_k=3,
+            make=lambda: datagen.er_3300(0), min_support=20, k=3, cpu=True,
             desc="Erdos-Renyi 3,300 V / 4,700 E, 6 uniform vertex labels, 1 edge label, seed 0"),
     }
 
@@ -96,15 +119,36 @@ def host_cores() -> int:
         return os.cpu_count() or 1
 
 
-def run_port(graph_path: str, min_support: int, k: int, cores: int) -> dict:
-    """One run of the CPU oracle port; returns its counts and fsm time."""
+def run_port(graph_path: str, min_support: int, k: int, cores: int, shard: tuple[int, int] | None = None) -> dict:
+    """One run of the CPU oracle port with its last level streamed (optionally
+    one slice of it); returns its counts and times."""
     port = os.path.join(ROOT, "oracle", "_port", "fsm_port")
     if not os.path.exists(port):
         subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
     env = dict(os.environ, OMP_NUM_THREADS=str(cores), CUDA_VISIBLE_DEVICES="")
-    r = subprocess.run([port, graph_path, str(min_support), str(k), "--stats"], capture_output=True, text=True,
-                       check=True, env=env)
-    return json.loads(r.stderr.strip().splitlines()[-1])
+    args = [port, graph_path, str(min_support), str(k), "--stats", "--stream-last"]
+    if shard:
+        args += ["--shard", f"{shard[0]}/{shard[1]}"]
+    r = subprocess.run(args, capture_output=True, text=True, check=True, env=env)
+    out = json.loads(r.stderr.strip().splitlines()[-1])
+    out["lines"] = r.stdout.splitlines()[:-1]
+    return out
+
+
+NO_CPU = "the CPU port needs hours for this job (about 4e12 extended embeddings at 3 edges)"
+
+
+def cpu_sample(graph_path: str, wl: dict, cores: int, slices: int = 4) -> dict:
+    """cpu_baseline: the port on the levels above the last plus one slice of
+    `slices` of the last level, scaled to a whole job."""
+    r = run_port(graph_path, wl["min_support"], wl["k"], cores, shard=(0, slices))
+    upper = r["fsm_s"] - r["last_s"]
+    job_ms = 1e3 * (upper + slices * r["last_s"])
+    return {"value": job_ms, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{wl['desc']}; min support {wl['min_support']}; {wl['k']} edges; every level above the "
+                      f"last ({upper:.3f} s) plus slice 1 of {slices} of the last level's parent embeddings "
+                      f"({r['last_extended']} extended embeddings in {r['last_s']:.3f} s), last level scaled "
+                      f"x{slices}; oracle port, OpenMP, last level streamed"}
 
 
 class ClockSampler:
@@ -176,6 +220,25 @@ def replica_value(world: int, units_per_rank: float, slowest_ms: float) -> float
     return world * units_per_rank / (slowest_ms / 1e3)
 
 
+def replica_ms_per_job(world: int, jobs_per_rank: int, slowest_ms: float) -> float:
+    """Whole-job time per job of `world` replicas: the slowest rank's time over
+    the jobs all ranks completed."""
+    return slowest_ms / (world * jobs_per_rank)
+
+
+def measured_traffic(workload: str, kernel: str):
+    """DRAM bytes per launch of `kernel` on `workload` from an ncu capture
+    (profiles/dram_traffic.json), or None when none was taken."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if not os.path.exists(path):
+        return None, None
+    with open(path) as f:
+        rec = json.load(f).get(workload)
+    if not rec or not kernel.startswith(rec["kernel"]):
+        return None, None
+    return rec["bytes_per_launch"], rec["source"]
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -187,32 +250,38 @@ def reference_arm(args, wl) -> None:
     world, rank, _ = dist_setup()
     if rank != 0:
         return
-    if wl["sample_k"] is None:
-        print(json.dumps({"impl": "reference", "unavailable": "the CPU port would hold about 1e10 two-edge "
-                                                              "embeddings of this graph in host memory"}), flush=True)
+    if not wl["cpu"]:
+        print(json.dumps({"impl": "reference", "unavailable": NO_CPU}), flush=True)
         return
     cores = host_cores()
     g = wl["make"]()
+    slices = max(args.steps, 1)
     with tempfile.TemporaryDirectory() as tmp:
         path = os.path.join(tmp, "g.bin")
         g.save(path)
-        for _ in range(args.warmup):
-            run_port(path, wl["min_support"], wl["sample_k"], cores)
-        runs = [run_port(path, wl["min_support"], wl["sample_k"], cores) for _ in range(args.steps)]
-    ext = sum(r["extended"] for r in runs)
-    secs = sum(r["fsm_s"] for r in runs)
-    value = ext / secs if secs > 0 else 0.0
-    sample = (f"{wl['desc']}; min support {wl['min_support']}; patterns up to {wl['sample_k']} edges "
-              f"(bounded sample of the {wl['k']}-edge job); oracle port, OpenMP")
+        for w in range(args.warmup):
+            run_port(path, wl["min_support"], wl["k"], cores, shard=(w % slices, slices))
+        runs = [run_port(path, wl["min_support"], wl["k"], cores, shard=(i, slices)) for i in range(slices)]
+    upper_s = statistics.median(r["fsm_s"] - r["last_s"] for r in runs)
+    last_s = sum(r["last_s"] for r in runs)
+    job_ms = 1e3 * (upper_s + last_s)
+    upper_ext = runs[0]["extended"] - runs[0]["last_extended"]
+    assert all(r["extended"] - r["last_extended"] == upper_ext for r in runs), "levels above the last differ"
+    extended = upper_ext + sum(r["last_extended"] for r in runs)
+    sample = (f"{wl['desc']}; min support {wl['min_support']}; {wl['k']} edges; step i = every level above the "
+              f"last plus slice i of {slices} of the last level's parent embeddings; the slices cover the last "
+              f"level once; oracle port, OpenMP, last level streamed")
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(runs), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "impl": "reference", "metric": METRIC, "value": job_ms, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(r["fsm_s"] for r in runs),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator)",
         "config": {"workload": args.workload, "description": wl["desc"], "min_support": wl["min_support"],
-                   "k": wl["sample_k"], "parallelism": "cpu"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "extended_per_step": runs[0]["extended"], "patterns": runs[0]["patterns"],
+                   "k": wl["k"], "parallelism": "cpu"},
+        "cpu_baseline": {"value": job_ms, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": job_ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "embeddings_per_s": extended / (job_ms / 1e3), "extended_per_job": extended,
+        "job_ms_parts": {"above_last_level_median": 1e3 * upper_s, "last_level_sum": 1e3 * last_s},
     }
     print(json.dumps(line), flush=True)
 
@@ -245,17 +314,13 @@ def gpu_arm(args, wl) -> None:
     h2d_graph = off_h.numel() * 4 + vl_h.numel() * 4 + ed_h.numel() * 4
 
     cpu = None
-    if wl["sample_k"] is None:
-        cpu = {"unavailable": "the CPU port would hold about 1e10 two-edge embeddings of this graph in host memory"}
+    if not wl["cpu"]:
+        cpu = {"unavailable": NO_CPU}
     elif rank == 0 and world == 1 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as tmp:
             path = os.path.join(tmp, "g.bin")
             g.save(path)
-            cores = host_cores()
-            r = run_port(path, sup, wl["sample_k"], cores)
-        cpu = {"value": r["extended"] / r["fsm_s"], "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{wl['desc']}; min support {sup}; patterns up to {wl['sample_k']} edges "
-                         f"({r['extended']} extended embeddings in {r['fsm_s']:.3f} s); oracle port, OpenMP"}
+            cpu = cpu_sample(path, wl, host_cores())
 
     with Miner(device=local, profile=True) as m:
         with ClockSampler(local, settle_s=1.0) as clk:
@@ -302,8 +367,8 @@ def gpu_arm(args, wl) -> None:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
-    value = replica_value(world, ext, total_ms)
-    e2e_value = replica_value(world, ext, e2e_total)
+    value = replica_ms_per_job(world, len(step_ms), total_ms)
+    e2e_value = replica_ms_per_job(world, len(e2e_ms), e2e_total)
     # Dominant kernel family by CUDA-event time over the timed steps.
     fams = {"k_mask_rows (mask path row pass)": ("rows_ms", "rows_bytes", "rows_launches"),
             "k_expand Count/Support (per-candidate path)": ("expand_ms", "expand_bytes", "expand_launches"),
@@ -318,14 +383,10 @@ def gpu_arm(args, wl) -> None:
         peaks = json.load(f)
     peak = peaks.get("hbm_gbs") or 6800.0
     achieved = exp_bytes / (exp_ms / 1e3) / 1e9 if exp_ms > 0 else 0.0
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "expand_traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(args.workload)
+    traffic, traffic_source = measured_traffic(args.workload, dom)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / len(step_ms), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": total_ms / len(step_ms), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
         "config": {"workload": args.workload, "description": wl["desc"], "min_support": sup, "k": k,
                    "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
@@ -334,12 +395,16 @@ def gpu_arm(args, wl) -> None:
                 "h2d_bytes_per_step": int(h2d_graph + stats[-1]["h2d_bytes"]),
                 "d2h_bytes_per_step": int(statistics.median(e2e_d2h))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "frac": achieved / peak if peak else None, "traffic": traffic, "traffic_source": traffic_source,
                      "kernel": dom, "launches_per_step": exp_launches / len(stats),
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "cpu_baseline": cpu,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "clocks": clocks,
+        "embeddings_per_s": {"value": replica_value(world, ext, total_ms),
+                             "e2e": replica_value(world, ext, e2e_total), "unit": EMB_UNIT,
+                             "note": "counted, not enumerated: the mask path sums most children per adjacency "
+                                     "segment instead of producing them one by one"},
         "extended_per_step": stats[-1]["extended"], "patterns": stats[-1]["patterns"],
         "mining_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
         "kernel_ms_per_step": {**{name: ms / len(stats) for name, ms in fam_ms.items()},
@@ -517,6 +582,14 @@ def text_arm(args) -> None:
         src, dst = os.path.join(tmp, "g.txt"), os.path.join(tmp, "g.bin")
         with open(src, "wb") as f:
             f.write(text)
+        # Outside the timed region: both loaders must give the same graph, as
+        # seen by mining it (every pattern and support at 2 edges).
+        subprocess.run([convert, src, dst], check=True, capture_output=True)
+        dg_text, dg_host = m.upload_text(text), m.upload(datagen.load_bin(dst))
+        same = m.mine(dg_text, 2, 10000)[0] == m.mine(dg_host, 2, 10000)[0]
+        m.free(dg_text)
+        m.free(dg_host)
+        assert same, "device text loader and host reader give different graphs"
         for step in range(args.warmup + args.steps):
             t = time.perf_counter()
             dg = m.upload_text(text)
@@ -535,7 +608,7 @@ def text_arm(args) -> None:
         "value": statistics.median(dev_ms), "unit": "ms", "higher_is_better": False, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "data": "synthetic (seeded generator)",
         "config": {"workload": "text_load", "description": "chung_lu_100k as gSpan text",
-                   "text_bytes": len(text)},
+                   "text_bytes": len(text)}, "same_graph_checked": True,
         "host_ms": statistics.median(host_ms)}), flush=True)
 
 

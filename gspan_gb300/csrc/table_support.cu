@@ -64,6 +64,16 @@ __global__ void k_table_min(int32_t ncols, uint32_t* out)
     out[ncols] = best;
 }
 
+// The error of launches just made, cleared once taken.  Callers check with
+// cudaPeekAtLastError before launching that no error of earlier, unrelated work
+// is pending, so an error seen here is this call's own.
+cudaError_t take_launch_error()
+{
+    const cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) cudaGetLastError();
+    return e;
+}
+
 cudaError_t launch_table(const TableCols& t, int32_t ncols, int64_t nrows, int32_t n, uint32_t* bits,
                          uint32_t* out, uint32_t* status, cudaStream_t st)
 {
@@ -78,7 +88,7 @@ cudaError_t launch_table(const TableCols& t, int32_t ncols, int64_t nrows, int32
     }
     k_table_sizes<<<ncols, 256, 0, st>>>(words, bits, out);
     k_table_min<<<1, 1, 0, st>>>(ncols, out);
-    return cudaGetLastError();
+    return take_launch_error();
 }
 
 gspan_status check_table_args(int32_t nr_nodes, const int32_t* const* cols, int32_t ncols, int64_t nrows,
@@ -104,6 +114,8 @@ extern "C" gspan_status gspan_table_support(gspan_ctx* ctx, int32_t nr_nodes, co
         return gs::fail(ctx, GSPAN_ERR_INVALID, "table support: bad arguments (1..16 columns, nr_nodes >= 1)");
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return gs::cuda_fail(ctx, e, "set device");
+    if ((e = cudaPeekAtLastError()) != cudaSuccess)   // left pending by earlier work: not ours to clear
+        return gs::cuda_fail(ctx, e, "table support: an earlier CUDA error is pending on this thread");
     cudaStream_t s = ctx->stream;
     const size_t words = ((size_t)nr_nodes + 31) / 32;
     uint32_t* bits = nullptr;
@@ -139,6 +151,11 @@ extern "C" gspan_status gspan_table_support(gspan_ctx* ctx, int32_t nr_nodes, co
 // Every call uses the same array and leaves its bitmaps behind; each call
 // clears the part it uses before filling it.  Calls whose work overlaps on
 // the GPU (another stream, another host thread) race on the array.
+//
+// The call launches its kernels and returns without waiting.  If an error of
+// earlier work is already pending on the calling thread (cudaPeekAtLastError),
+// it launches nothing, leaves that error for its owner and returns
+// GSPAN_ERR_CUDA; otherwise GSPAN_ERR_CUDA means one of its own launches failed.
 
 namespace gs {
 namespace {
@@ -201,6 +218,7 @@ extern "C" gspan_status gspan_table_support_noalloc(int32_t nr_nodes, const int3
     uint32_t* scratch = nullptr;
     const gspan_status rc = gs::scratch_for(dev, &scratch);
     if (rc != GSPAN_OK) return rc;
+    if (cudaPeekAtLastError() != cudaSuccess) return GSPAN_ERR_CUDA;   // earlier work's error, left pending
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     uint32_t* flag = scratch;
     uint32_t* bits = scratch + gs::kNoAllocHeaderWords;
@@ -215,5 +233,5 @@ extern "C" gspan_status gspan_table_support_noalloc(int32_t nr_nodes, const int3
     }
     gs::k_table_sizes<<<ncols, 256, 0, s>>>((uint32_t)words, bits, out);
     gs::k_table_min_flagged<<<1, 1, 0, s>>>(ncols, flag, out);
-    return cudaGetLastError() == cudaSuccess ? GSPAN_OK : GSPAN_ERR_CUDA;
+    return gs::take_launch_error() == cudaSuccess ? GSPAN_OK : GSPAN_ERR_CUDA;
 }

@@ -265,7 +265,9 @@ gspan_status gspan_table_support(gspan_ctx* ctx, int32_t nr_nodes, const int32_t
  *     asynchronous call; out[ncols] is then 0xFFFFFFFF.
  *   - The first call on a device looks up the array's device address; make
  *     that first call before any stream capture on that device.
- *   - All calls share the array: calls whose GPU work overlaps race. */
+ *   - All calls share the array: calls whose GPU work overlaps race.
+ *   - If a CUDA error of earlier work is pending on the calling thread, the
+ *     call launches nothing, leaves that error in place and returns CUDA. */
 gspan_status gspan_table_support_noalloc(int32_t nr_nodes, const int32_t* const* cols, int32_t ncols,
                                          int64_t nrows, uint32_t* out, void* stream);
 

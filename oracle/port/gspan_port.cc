@@ -10,6 +10,7 @@
 #include "gspan_port.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <map>
 #include <omp.h>
@@ -350,12 +351,177 @@ void extend_all(const Graph& g, const Code& code, const Layers& layers, const st
     }
 }
 
+// ---------------------------------------------------------------------------
+// Streaming last level.  Children of a pattern with k-1 edges are leaves of the
+// search: the reference materialises them (gspan.cu:1131-1138), walks each
+// child's layers for its MNI domains (gspan.cu:165-190, 255-260), reports it and
+// stops at |code| >= k (gspan.cu:1128).  A child embedding's images are its
+// parent embedding's images plus, for a forward child, the new neighbour.  So
+// for each child (v_i, el[, tl]) the domain of an old pattern vertex p is
+// {img_r(p) : parent row r has at least one such child}, and the new vertex's
+// domain is the set of new neighbours.  One pass over the parent rows, with the
+// same three rules as extend_all, accumulates exactly those sets and counts.
+
+// Dense ranks of the labels present, so child tuples index flat arrays; rank
+// order is label order, so every `<` of the reference is kept.
+struct Ranks {
+    std::vector<int> vlab, elab;          // sorted distinct labels
+    std::vector<int> vr, er;              // rank per vertex / per directed entry
+    explicit Ranks(const Graph& g)
+    {
+        vlab = g.vlabels;
+        std::sort(vlab.begin(), vlab.end());
+        vlab.erase(std::unique(vlab.begin(), vlab.end()), vlab.end());
+        for (const Edge& e : g.edges) elab.push_back(e.label);
+        std::sort(elab.begin(), elab.end());
+        elab.erase(std::unique(elab.begin(), elab.end()), elab.end());
+        vr.resize(g.n);
+        for (int v = 0; v < g.n; ++v)
+            vr[v] = (int)(std::lower_bound(vlab.begin(), vlab.end(), g.vlabels[v]) - vlab.begin());
+        er.resize(g.m);
+        for (int i = 0; i < g.m; ++i)
+            er[i] = (int)(std::lower_bound(elab.begin(), elab.end(), g.edges[i].label) - elab.begin());
+    }
+};
+
+inline void set_bit(uint64_t* w, uint32_t v)
+{
+    const uint64_t b = (uint64_t)1 << (v % 64);
+    if (!(__atomic_load_n(&w[v / 64], __ATOMIC_RELAXED) & b)) __atomic_fetch_or(&w[v / 64], b, __ATOMIC_RELAXED);
+}
+
+// The slice of a parent row: a hash of the data edge id of its last layer, so
+// that it does not depend on the row's position (the order of rows inside a
+// materialised layer follows thread timing).
+inline int row_shard(const Rels& last, long long idx, int count)
+{
+    uint64_t h = ((uint64_t)(uint32_t)last[idx].eid + 0x9E3779B97F4A7C15ull) * 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 31;
+    return (int)(h % (uint64_t)count);
+}
+
+inline int min_domain(const uint64_t* bits, int nverts, size_t words)
+{
+    int sup = 0x7fffffff;
+    for (int p = 0; p < nverts; ++p) {
+        long long c = 0;
+        for (size_t w = 0; w < words; ++w) c += __builtin_popcountll(bits[(size_t)p * words + w]);
+        if (c > 0 && c < sup) sup = (int)c;
+    }
+    return sup;
+}
+
 struct Miner {
     const Graph& g;
     int k, min_support;
     const ReportFn& report;
     Stats& st;
     std::vector<uint64_t> bits;
+    bool stream_last = false;
+    const Ranks* ranks = nullptr;
+    Shard shard;
+
+    // The leaves below `code` (which has k-1 edges), reported in the order the
+    // recursion of mine() visits them.
+    void stream_children(Code& code, const Layers& layers, const std::vector<int>& rm)
+    {
+        const Ranks& R = *ranks;
+        const int NE = (int)R.elab.size(), NV = (int)R.vlab.size();
+        int nv = 0;
+        for (const PEdge& e : code) nv = std::max(nv, std::max(e.from, e.to) + 1);
+        const int v_n = code[rm[0]].to;
+        const int min_label = code[0].fl;
+        const size_t words = ((size_t)g.n + 63) / 64;
+        const int nb = nv * NE, nf = nv * NE * NV;
+        // Domains: a backward child has nv pattern vertices, a forward one nv+1.
+        std::vector<uint64_t> bb((size_t)nb * nv * words, 0), bf((size_t)nf * (nv + 1) * words, 0);
+        std::vector<uint64_t> cb(nb, 0), cf(nf, 0);
+        const Rels& last = *layers.back();
+        const auto t0 = std::chrono::steady_clock::now();
+
+        #pragma omp parallel
+        {
+            History hist;
+            std::vector<int> img(nv);
+            std::vector<uint64_t> lb(nb, 0), lf(nf, 0);
+            std::vector<long long> stamp_b(nb, -1), stamp_f(nf, -1);
+            std::vector<int> touched_b, touched_f;
+            #pragma omp for schedule(guided)
+            for (long long ei = 0; ei < (long long)last.size(); ++ei) {
+                if (shard.count > 1 && row_shard(last, ei, shard.count) != shard.index) continue;
+                build_history(g, layers, (int)ei, hist);
+                img[0] = hist.h[0].from;
+                for (size_t i = 0; i < code.size(); ++i)
+                    if (code[i].forward()) img[code[i].to] = hist.h[i].to;
+                const int u_n = hist.h[rm[0]].to;
+                touched_b.clear();
+                touched_f.clear();
+                for (int i = (int)rm.size() - 1; i >= 1; --i) {
+                    const int kk = rm[i];
+                    int idx;
+                    if (backward_edge(g, hist.h[kk], u_n, hist, &idx)) {
+                        const int key = code[kk].from * NE + R.er[idx];
+                        ++lb[key];
+                        if (stamp_b[key] != ei) { stamp_b[key] = ei; touched_b.push_back(key); }
+                    }
+                }
+                auto fwd = [&](int v_i) {
+                    return [&, v_i](int, int, int idx) {
+                        const int to = g.edges[idx].to;
+                        const int key = (v_i * NE + R.er[idx]) * NV + R.vr[to];
+                        ++lf[key];
+                        set_bit(&bf[((size_t)key * (nv + 1) + nv) * words], (uint32_t)to);
+                        if (stamp_f[key] != ei) { stamp_f[key] = ei; touched_f.push_back(key); }
+                    };
+                };
+                first_forward(g, u_n, min_label, hist, fwd(v_n));
+                for (size_t i = 0; i < rm.size(); ++i)
+                    other_forward(g, hist.h[rm[i]], min_label, hist, fwd(code[rm[i]].from));
+                for (int key : touched_b)
+                    for (int p = 0; p < nv; ++p) set_bit(&bb[((size_t)key * nv + p) * words], (uint32_t)img[p]);
+                for (int key : touched_f)
+                    for (int p = 0; p < nv; ++p)
+                        set_bit(&bf[((size_t)key * (nv + 1) + p) * words], (uint32_t)img[p]);
+            }
+            #pragma omp critical
+            {
+                for (int q = 0; q < nb; ++q) cb[q] += lb[q];
+                for (int q = 0; q < nf; ++q) cf[q] += lf[q];
+            }
+        }
+        st.last_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+
+        auto leaf = [&](const PEdge& pe, uint64_t count, const uint64_t* dom, int nverts) {
+            st.extended += count;
+            st.last_extended += count;
+            code.push_back(pe);
+            if (is_canonical(code)) {
+                ++st.support_calls;
+                const int sup = min_domain(dom, nverts, words);
+                if (sup >= min_support) {
+                    ++st.patterns;
+                    report(code, sup);
+                }
+            }
+            code.pop_back();
+        };
+        // Backward children: ascending (v_i, edge label).
+        for (int v_i = 0; v_i < nv; ++v_i)
+            for (int e = 0; e < NE; ++e) {
+                const int key = v_i * NE + e;
+                if (cb[key])
+                    leaf(PEdge{v_n, v_i, -1, R.elab[e], -1}, cb[key], &bb[(size_t)key * nv * words], nv);
+            }
+        // Forward children: descending v_i, then ascending (edge label, to label).
+        for (int v_i = nv - 1; v_i >= 0; --v_i)
+            for (int e = 0; e < NE; ++e)
+                for (int t = 0; t < NV; ++t) {
+                    const int key = (v_i * NE + e) * NV + t;
+                    if (cf[key])
+                        leaf(PEdge{v_i, v_n + 1, -1, R.elab[e], R.vlab[t]}, cf[key],
+                             &bf[(size_t)key * (nv + 1) * words], nv + 1);
+                }
+    }
 
     // Pre-order recursion (gspan.cu:1118-1169).
     void mine(Code& code, Layers& layers)
@@ -370,6 +536,10 @@ struct Miner {
 
         const std::vector<int> rm = rightmost_path(code);
         const int v_n = code[rm[0]].to;
+        if (stream_last && (int)code.size() + 1 == k) {
+            stream_children(code, layers, rm);
+            return;
+        }
         BackMap back;
         FwdMap fwd;
         extend_all(g, code, layers, rm, back, fwd);
@@ -411,13 +581,15 @@ bool is_canonical(const Code& code)
     return projection_is_canonical(p, it->second, code, min_code);
 }
 
-void mine_all(const Graph& g, int k, int min_support, const ReportFn& report, Stats* stats)
+void mine_all(const Graph& g, int k, int min_support, const ReportFn& report, Stats* stats, bool stream_last,
+              Shard shard)
 {
     Stats local;
     Stats& st = stats ? *stats : local;
     std::map<SeedKey, Rels> seeds;
     for_each_seed(g, [&](const SeedKey& key, int i) { seeds[key].push_back(Rel{-1, i}); });
-    Miner miner{g, k, min_support, report, st, {}};
+    const Ranks ranks(g);
+    Miner miner{g, k, min_support, report, st, {}, stream_last, &ranks, shard};
     for (auto& s : seeds) {
         st.seeds += s.second.size();
         Code code{PEdge{0, 1, s.first.fl, s.first.el, s.first.tl}};

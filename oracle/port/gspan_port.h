@@ -37,12 +37,30 @@ struct Stats {
     uint64_t extended = 0;       // child embeddings produced by extension
     uint64_t patterns = 0;       // reported patterns
     uint64_t support_calls = 0;  // canonical candidates whose support was counted
+    double last_s = 0;           // seconds spent counting a streamed last level
+    uint64_t last_extended = 0;  // the part of `extended` in a streamed last level
+};
+
+// A slice of a streamed last level: only parent rows whose last data edge
+// hashes to `index` modulo `count` are extended.  Counts and times of the `count` slices add up to the whole
+// level's; supports and reports are then partial (timing use only).
+struct Shard {
+    int index = 0, count = 1;
 };
 
 using ReportFn = std::function<void(const Code&, int support)>;
 
 // Runs the whole mining job; calls `report` in the reference's pre-order.
-void mine_all(const Graph& g, int k, int min_support, const ReportFn& report, Stats* stats);
+//
+// stream_last = false extends every level as the reference does: the children
+// of a pattern are materialised as {prev_idx, edge_id} layers
+// (gspan.cu:1131-1138), then each child's support walks them.
+// stream_last = true changes only how the last level (patterns of k edges) is
+// counted: each parent embedding's children are produced by the same three
+// rules and ORed straight into per-child domain bitsets, never stored.  Output
+// and counts are identical; memory no longer grows with the last level.
+void mine_all(const Graph& g, int k, int min_support, const ReportFn& report, Stats* stats,
+              bool stream_last = false, Shard shard = Shard{});
 
 // The minimum-DFS-code test of gspan.cu:586-606 on its own (for unit tests).
 bool is_canonical(const Code& code);

@@ -9,6 +9,17 @@ from gspan_gb300.datagen by the tests, and the sha256 of their binary CSR
 file is stored to catch generator drift.
 
     python tests/golden/make_golden.py
+
+Large cases (``--large``): jobs whose last level the reference would have to
+materialise in host memory beyond any test host (the 100,000-vertex Chung-Lu
+graph at 3 edges holds about 1.9e10 three-edge embeddings).  Their lines come
+from the oracle port with ``--stream-last``: the same rules and support
+semantics, the last level counted without storing it.  That mode is checked
+against the reference's own output on every small case above
+(tests/test_oracle.py) before it is trusted here.  Written to
+large_manifest.json with the job's extended-embedding count.
+
+    python tests/golden/make_golden.py --large
 """
 import hashlib
 import json
@@ -41,6 +52,38 @@ CASES = [
 ]
 
 
+# (name, generator call, min_support, k)
+LARGE_CASES = [
+    ("chung_lu_100k", "datagen.chung_lu_100k(1)", 10000, 3),
+]
+
+
+def make_large() -> None:
+    port = os.path.join(ROOT, "oracle", "_port", "fsm_port")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+    manifest = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, expr, sup, k in LARGE_CASES:
+            g = eval(expr, {"datagen": datagen})
+            path = os.path.join(tmp, name + ".bin")
+            g.save(path)
+            r = subprocess.run([port, path, str(sup), str(k), "--stats", "--stream-last"], capture_output=True,
+                               text=True, check=True)
+            out = r.stdout.splitlines()
+            assert out and out[-1].startswith("load:"), out[-1:]
+            st = json.loads(r.stderr.strip().splitlines()[-1])
+            fname = f"{name}_s{sup}_k{k}.txt"
+            with open(os.path.join(HERE, fname), "w") as f:
+                f.write("".join(line + "\n" for line in out[:-1]))
+            manifest.append({"name": name, "graph": expr, "sha256": hashlib.sha256(g.to_bytes()).hexdigest(),
+                             "min_support": sup, "k": k, "expected": fname, "patterns": len(out) - 1,
+                             "seeds": st["seeds"], "extended": st["extended"],
+                             "source": "oracle port, --stream-last"})
+    with open(os.path.join(HERE, "large_manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+        f.write("\n")
+
+
 def main() -> None:
     ref = os.path.join(ROOT, "oracle", "_ref", "fsm")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
@@ -66,4 +109,7 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    if "--large" in sys.argv[1:]:
+        make_large()
+    else:
+        main()

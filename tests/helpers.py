@@ -12,15 +12,17 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 PORT = os.path.join(ROOT, "oracle", "_port", "fsm_port")
 
 
-def run_port(g, min_support, k, threads=None, with_stats=False):
-    """Pattern lines of the oracle port (timing line removed), optionally with its counts."""
+def run_port(g, min_support, k, threads=None, with_stats=False, stream_last=False):
+    """Pattern lines of the oracle port (timing line removed), optionally with
+    its counts; stream_last counts the last level without materialising it."""
     env = dict(os.environ)
     if threads:
         env["OMP_NUM_THREADS"] = str(threads)
     with tempfile.TemporaryDirectory() as tmp:
         path = os.path.join(tmp, "g.bin")
         g.save(path)
-        args = [PORT, path, str(min_support), str(k)] + (["--stats"] if with_stats else [])
+        args = ([PORT, path, str(min_support), str(k)] + (["--stats"] if with_stats else [])
+                + (["--stream-last"] if stream_last else []))
         r = subprocess.run(args, capture_output=True, text=True, check=True, env=env)
     lines = r.stdout.splitlines()
     assert lines and lines[-1].startswith("load:")
@@ -31,6 +33,12 @@ def run_port(g, min_support, k, threads=None, with_stats=False):
 
 def golden_cases():
     with open(os.path.join(GOLDEN, "manifest.json")) as f:
+        return json.load(f)
+
+
+def large_golden_cases():
+    """Full-size jobs pinned by the streaming oracle (tests/golden/make_golden.py --large)."""
+    with open(os.path.join(GOLDEN, "large_manifest.json")) as f:
         return json.load(f)
 
 

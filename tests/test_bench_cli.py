@@ -24,11 +24,23 @@ def test_workloads_listed():
 
 
 def test_reference_arm_line():
-    line = run_bench("--impl", "reference", "--workload", "er_3300", "--steps", "1", "--warmup", "0")
-    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "embeddings/s"
-    assert line["higher_is_better"] is True and line["e2e"]["h2d_bytes_per_step"] == 0
+    """Same job, metric and unit as the GPU arm: milliseconds per job at 3 edges,
+    the last level timed in slices that add up to the whole job."""
+    line = run_bench("--impl", "reference", "--workload", "er_3300", "--steps", "3", "--warmup", "1")
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "ms/job"
+    assert line["higher_is_better"] is False and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["config"]["k"] == 3 and line["config"]["workload"] == "er_3300"
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
-    assert line["extended_per_step"] > 0
+    assert line["extended_per_job"] == 91207   # the whole k = 3 job (tests/test_oracle.py)
+
+
+def test_reference_arm_loads_no_native_library():
+    """The reference arm never maps this repository's libgspan_gb300.so."""
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'er_3300', "
+            "'--steps', '1', '--warmup', '0']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); assert 'libgspan_gb300' not in maps, 'library mapped'")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
 
 
 def test_reference_arm_unavailable_where_the_port_cannot_run():

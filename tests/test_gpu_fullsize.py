@@ -1,15 +1,18 @@
 """The headline job at full size (Chung-Lu 100,000 vertices / 1,080,000 edges,
 min support 10,000, up to 3 edges).  The reference cannot run it: the
 3-edge level has about 1.9e10 embeddings, which it materialises in host RAM.
-Parity therefore rests on properties that do not depend on the size:
-  * the patterns with at most 2 edges equal the oracle's run at k = 2,
-    supports included, and the embedding counts of that run agree;
-  * both extension paths agree on every line and every count at k = 3;
+Parity is pinned by the oracle port counting that level without storing it
+(tests/golden/chung_lu_100k_s10000_k3.txt, made by make_golden.py --large; the
+streaming mode equals the reference's own output on every small golden case):
+  * every line, support included, and the extended-embedding count equal the
+    fixture on each kernel path;
+  * the patterns with at most 2 edges equal the oracle's run at k = 2, and the
+    embedding counts of that run agree;
   * MNI support is anti-monotone: a child's support never exceeds its parent's;
   * repeated runs are identical."""
 import pytest
 
-from helpers import lines_of, run_port
+from helpers import golden_lines, large_golden_cases, lines_of, run_port
 
 pytestmark = pytest.mark.gpu
 
@@ -30,6 +33,15 @@ def runs(graph):
             out[path] = [m.mine(dg, 3, 10000), m.mine(dg, 2, 10000)]
             m.free(dg)
     return out
+
+
+def test_matches_streaming_oracle_fixture(runs):
+    case = [c for c in large_golden_cases() if c["name"] == "chung_lu_100k" and c["k"] == 3][0]
+    want = golden_lines(case)
+    for path in (0, 1, 2):
+        patterns, st = runs[path][0]
+        assert lines_of(patterns) == want, f"path {path}"
+        assert st["extended"] == case["extended"] and st["seeds"] == case["seeds"], f"path {path}"
 
 
 def test_two_edge_prefix_matches_oracle(graph, runs):

@@ -45,6 +45,38 @@ def test_noalloc_matches_allocating_entry_point():
             assert sizes == [len(np.unique(h)) for h in host]
 
 
+def test_noalloc_flags_a_bad_id_then_recovers():
+    """An id outside [0, nr_nodes) sets out[ncols] to 0xFFFFFFFF (the call is
+    asynchronous and cannot return it); the flag word lives in the shared
+    array, so the next clean call must clear it and give the normal support."""
+    import torch
+    stream = torch.cuda.current_stream().cuda_stream
+    n = 1000
+    good = [torch.arange(0, 300, dtype=torch.int32, device="cuda") % (c + 7) for c in range(3)]
+    bad = [c.clone() for c in good]
+    bad[1][17] = n                                   # one id equal to nr_nodes
+    rc, out = _noalloc(bad, n, stream)
+    torch.cuda.current_stream().synchronize()
+    assert rc == 0 and (out[3].item() & 0xFFFFFFFF) == 0xFFFFFFFF
+    rc, out = _noalloc(good, n, stream)
+    torch.cuda.current_stream().synchronize()
+    assert rc == 0 and [v & 0xFFFFFFFF for v in out.cpu().tolist()] == [7, 8, 9, 7]
+
+
+def test_noalloc_empty_table():
+    """nrows == 0: every domain is empty and the support is 0x7fffffff, even
+    right after a call that left bits in the array."""
+    import torch
+    stream = torch.cuda.current_stream().cuda_stream
+    full = [torch.arange(0, 500, dtype=torch.int32, device="cuda") for _ in range(2)]
+    rc, _ = _noalloc(full, 500, stream)
+    assert rc == 0
+    empty = [torch.empty(0, dtype=torch.int32, device="cuda") for _ in range(2)]
+    rc, out = _noalloc(empty, 500, stream)
+    torch.cuda.current_stream().synchronize()
+    assert rc == 0 and out.cpu().tolist() == [0, 0, 0x7fffffff]
+
+
 def test_noalloc_rejects_tables_beyond_its_array():
     import torch
     cols = [torch.zeros(4, dtype=torch.int32, device="cuda")] * 16
