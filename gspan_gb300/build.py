@@ -27,7 +27,7 @@ LIB = os.path.join(OUT, "libgspan_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["kernels.cu", "table_support.cu", "miner.cc", "capi.cc", "canonical.cc", "host_graph.cc",
-           "host_fsm.cc", "graph_store.cc", "server.cc", "autotune.cc", "results.cc", "text_loader.cu"]
+           "host_fsm.cc", "graph_store.cc", "server.cc", "autotune.cc", "results.cc", "text_loader.cu", "prune.cu"]
 TOOLS = {"fsm": "tools/fsm_main.cc", "convert": "tools/convert_main.cc"}
 
 

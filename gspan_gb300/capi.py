@@ -46,7 +46,8 @@ class GspanError(RuntimeError):
 class Opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("domain_mode", ctypes.c_int32),
                 ("hash_threshold", ctypes.c_double), ("mem_fraction", ctypes.c_double),
-                ("profile", ctypes.c_int32), ("path", ctypes.c_int32), ("mask_bias", ctypes.c_double)]
+                ("profile", ctypes.c_int32), ("path", ctypes.c_int32), ("mask_bias", ctypes.c_double),
+                ("prune", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -64,7 +65,8 @@ class Stats(ctypes.Structure):
                 ("materialize_ms", ctypes.c_double), ("materialize_launches", ctypes.c_uint64),
                 ("materialize_bytes", ctypes.c_double),
                 ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double),
-                ("canonical_checks", ctypes.c_uint64), ("canonical_ms", ctypes.c_double)]
+                ("canonical_checks", ctypes.c_uint64), ("canonical_ms", ctypes.c_double),
+                ("pruned_vertices", ctypes.c_uint64), ("pruned_entries", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -238,7 +240,8 @@ class Miner:
     """One mining context on one GPU (a CUDA stream and the device memory it owns)."""
 
     def __init__(self, device: int = 0, domain_mode: int = 0, hash_threshold: float = 1.0,
-                 profile: bool = False, mem_fraction: float = 0.85, path: int = 0, mask_bias: float = 1.0):
+                 profile: bool = False, mem_fraction: float = 0.85, path: int = 0, mask_bias: float = 1.0,
+                 prune: bool = False):
         opts = Opts()
         _lib.gspan_opts_default(ctypes.byref(opts))
         opts.device = device
@@ -248,6 +251,7 @@ class Miner:
         opts.mem_fraction = mem_fraction
         opts.path = path
         opts.mask_bias = mask_bias
+        opts.prune = 1 if prune else 0
         self._ctx = ctypes.c_void_p()
         rc = _lib.gspan_ctx_create(ctypes.byref(opts), ctypes.byref(self._ctx))
         if rc != GSPAN_OK:

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
+#include <string>
 #include <unordered_map>
 
 void Graph::add_vertex(int u, int label)
@@ -20,29 +21,54 @@ void Graph::add_edge(int u, int v, int label)
     (*this)[v].edges.push_back(Edge{v, u, label});
 }
 
-// Token-driven like graph.cc:38-64: a token starting with 't' is followed by
-// two tokens (ignored), 'v' by id and label, 'e' by both ends and the label;
-// any other token is skipped.  Vertices named only by edges get label 0.
+// Reads like graph.cc:38-64, with the same scanf calls: a token starting
+// with 't' is followed by one token (ignored) and an integer, 'v' by id and
+// label, 'e' by both ends and the label; any other token is skipped.  Vertices
+// named only by edges get label 0.
+//
+// Malformed records are read the reference's way.  Its three integers u, v, w
+// live across records ('t' writes u; 'v' writes v, w; 'e' writes u, v, w), and
+// a conversion that fails leaves its variable and the record's later ones as
+// the previous record left them: the record is still added with those values,
+// and the offending token is read as the next record's head.  A record that
+// would use a variable no earlier record assigned (uninitialised in the
+// reference, so its result is undefined) is refused with an exception.
+// Tokens of 16 or more characters, and a 't' record's skipped token of 4 or
+// more, overflow the reference's buffers (also undefined); here they are read
+// as whole tokens of up to 63 characters.
 Graph Graph::from_txt(const char* filename)
 {
     FILE* f = std::fopen(filename, "r");
     if (!f) throw std::runtime_error("failed to open file\n");
     Graph g;
     char tok[64];
+    int u = 0, v = 0, w = 0;
+    bool has_u = false, has_v = false, has_w = false;
     long nr_edges = 0;
+    auto need = [&](bool ok, const char* what) {
+        if (!ok) {
+            std::fclose(f);
+            throw std::runtime_error(std::string("malformed record: ") + what +
+                                     " is read before any record assigned it");
+        }
+    };
     while (std::fscanf(f, "%63s", tok) == 1) {
         if (tok[0] == 't') {
             char skip[64];
-            int id;
-            if (std::fscanf(f, "%63s%d", skip, &id) != 2) break;
+            if (std::fscanf(f, "%63s%d", skip, &u) == 2) has_u = true;
         } else if (tok[0] == 'v') {
-            int v, label;
-            if (std::fscanf(f, "%d%d", &v, &label) != 2) break;
-            g.add_vertex(v, label);
+            const int got = std::fscanf(f, "%d%d", &v, &w);
+            has_v |= got >= 1;
+            has_w |= got >= 2;
+            need(has_v && has_w, "a vertex id or label");
+            g.add_vertex(v, w);
         } else if (tok[0] == 'e') {
-            int u, v, label;
-            if (std::fscanf(f, "%d%d%d", &u, &v, &label) != 3) break;
-            g.add_edge(u, v, label);
+            const int got = std::fscanf(f, "%d%d%d", &u, &v, &w);
+            has_u |= got >= 1;
+            has_v |= got >= 2;
+            has_w |= got >= 3;
+            need(has_u && has_v && has_w, "an edge end or label");
+            g.add_edge(u, v, w);
             ++nr_edges;
         }
     }

@@ -1037,6 +1037,29 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<in
     // set-up); here it is an argument error.
     if (k < 1) return fail(ctx, GSPAN_ERR_INVALID, "k must be at least 1");
     if (k > kMaxE) return fail(ctx, GSPAN_ERR_LIMIT, "k exceeds the largest supported pattern size");
+    if (ctx->opts.prune && g.ninst == 1 && minsup[0] > 1) {
+        // Mine a copy of the store without the vertices of infrequent labels
+        // (prune.cu); patterns and supports are the same, the work is less.
+        gspan_graph* pruned = nullptr;
+        int64_t kv = 0, ke = 0;
+        gspan_status rc = prune_store(ctx, g, minsup[0], &pruned, &kv, &ke);
+        if (rc != GSPAN_OK) return rc;
+        if (pruned) {
+            ctx->opts.prune = 0;
+            rc = mine(ctx, pruned->g, k, minsup, emit, stats);
+            ctx->opts.prune = 1;
+            free_graph(pruned, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+            delete pruned;
+            --ctx->live_graphs;
+            if (stats) {
+                stats->pruned_vertices = (uint64_t)(g.n - kv);
+                stats->pruned_entries = (uint64_t)(g.m - ke);
+                stats->mine_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+            }
+            return rc;
+        }
+    }
     LiveBlocks live(ctx->stream, ctx->device);
     Run run{ctx, g, k, minsup};
     run.s = ctx->stream;

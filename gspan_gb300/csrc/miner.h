@@ -67,4 +67,9 @@ void free_graph(gspan_graph* gr, cudaStream_t st);
 gspan_status load_text(gspan_ctx* ctx, const char* text, int64_t len, gspan_graph** out, int32_t* nr_nodes,
                        int32_t* nr_edges);
 gspan_status cuda_fail(gspan_ctx* ctx, cudaError_t e, const char* what);
+// Label-frequency pruning (prune.cu): a new store of `g` without the vertices
+// whose label occurs on fewer than min_support vertices; *out stays null when
+// no vertex would be dropped (or for a batch).
+gspan_status prune_store(gspan_ctx* ctx, const DevGraph& g, int32_t min_support, gspan_graph** out,
+                         int64_t* kept_vertices, int64_t* kept_entries);
 }  // namespace gs

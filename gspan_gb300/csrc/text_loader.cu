@@ -5,18 +5,20 @@
 //
 // Semantics follow the token-driven reader: a token starting with 't' takes
 // a string and an integer, 'v' an id and a label, 'e' two ids and a label;
-// other tokens are skipped; the first integer that fails to parse (or a
-// record cut off by the end of the text) ends the reading.  Vertices are
-// created by any mention, label 0 until a 'v' record names one (the last one
-// wins), renumbered densely in ascending id order; every edge is entered at
-// both ends.  Whether a token is a record head depends on all tokens before
-// it; that is resolved exactly by a scan over per-token transition functions
-// of "arguments still owed" (0..3).
+// other tokens are skipped.  Vertices are created by any mention, label 0
+// until a 'v' record names one (the last one wins), renumbered densely in
+// ascending id order; every edge is entered at both ends.  Whether a token is
+// a record head depends on all tokens before it; that is resolved exactly by
+// a scan over per-token transition functions of "arguments still owed" (0..3).
 //
-// Character-level corner cases of a scanf-based reader that a token-level
-// parser cannot reproduce are refused (GSPAN_ERR_INVALID) instead of being
-// guessed at: an integer followed by other characters in one token ("12ab"),
-// an integer outside int32, or a token of 64 characters or more.
+// Text this token parser would not read exactly like the reference's
+// scanf-based reader is refused (GSPAN_ERR_INVALID), never guessed at or cut
+// short: a record whose integer fails to parse or that the end of the text
+// cuts off (the reference then reuses the previous record's values, which the
+// host reader reproduces), an integer followed by other characters in one
+// token ("12ab"), an integer outside int32, or a token of 64 characters or
+// more.  Everything else gives exactly the host reader's graph.
+#include "device_scan.cuh"
 #include "miner.h"
 
 #include <cstdint>
@@ -25,10 +27,6 @@
 namespace gs {
 namespace {
 
-constexpr unsigned kAll = 0xFFFFFFFFu;
-constexpr int kThreads = 256;
-constexpr int kPer = 8;                      // elements per thread in the scans
-constexpr int kChunk = kThreads * kPer;      // elements per scan block
 constexpr int kTokPer = 32;                  // tokens per thread in the head scan
 constexpr int kLongToken = 64;
 
@@ -37,34 +35,6 @@ enum : uint8_t { kIntOk = 0, kIntFail = 1, kIntBad = 2 };
 __device__ __forceinline__ bool is_space(uint8_t c)
 {
     return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r';
-}
-
-// Exclusive scan of one value per thread over a 256-thread block; *total
-// receives the block's sum.
-__device__ int64_t block_exclusive_scan(int64_t v, int64_t* total)
-{
-    __shared__ int64_t warp_sums[kThreads / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int64_t x = v;
-    for (int d = 1; d < 32; d <<= 1) {
-        const int64_t y = __shfl_up_sync(kAll, x, d);
-        if (lane >= d) x += y;
-    }
-    if (lane == 31) warp_sums[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        int64_t s = lane < kThreads / 32 ? warp_sums[lane] : 0;
-        for (int d = 1; d < 32; d <<= 1) {
-            const int64_t y = __shfl_up_sync(kAll, s, d);
-            if (lane >= d) s += y;
-        }
-        if (lane < kThreads / 32) warp_sums[lane] = s;
-    }
-    __syncthreads();
-    const int64_t base = w > 0 ? warp_sums[w - 1] : 0;
-    *total = warp_sums[kThreads / 32 - 1];
-    __syncthreads();
-    return base + x - v;
 }
 
 // ---- token starts: count per block, scan, write ----------------------------
@@ -96,35 +66,6 @@ __global__ void k_tok_write(const uint8_t* __restrict__ text, int64_t len, const
     int64_t at = block_off[blockIdx.x] + block_exclusive_scan(c, &total);
     for (int q = 0; q < kPer; ++q)
         if (i0 + q < len && token_start(text, i0 + q)) tok[at++] = (int32_t)(i0 + q);
-}
-
-// Exclusive scan of n int64 values in one block of 1024 threads (block sums
-// of the other scans: a few hundred thousand at most); out[n] = total.
-__global__ void k_scan_small(const int64_t* __restrict__ in, int64_t* __restrict__ out, int64_t n)
-{
-    __shared__ int64_t part[1024];
-    const int64_t per = (n + blockDim.x - 1) / blockDim.x;
-    const int64_t b = (int64_t)threadIdx.x * per, e = b + per < n ? b + per : n;
-    int64_t s = 0;
-    for (int64_t i = b; i < e; ++i) s += in[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int64_t run = 0;
-        for (unsigned t = 0; t < blockDim.x; ++t) {
-            const int64_t v = part[t];
-            part[t] = run;
-            run += v;
-        }
-        out[n] = run;
-    }
-    __syncthreads();
-    int64_t run = part[threadIdx.x];
-    for (int64_t i = b; i < e; ++i) {
-        const int64_t v = in[i];
-        out[i] = run;
-        run += v;
-    }
 }
 
 // ---- per-token facts ---------------------------------------------------------
@@ -241,7 +182,8 @@ __global__ void k_heads(const uint8_t* __restrict__ fn, int64_t ntok, const uint
 
 // ---- records ---------------------------------------------------------------------
 
-// Earliest record that ends the reading: (head index << 1) | unsupported.
+// Earliest record the loader refuses: (head index << 1) | character-level
+// (0: a field that is not an integer, or a record cut off by the end).
 __global__ void k_records_end(const uint8_t* __restrict__ text, const int32_t* __restrict__ tok, int64_t ntok,
                               const uint8_t* __restrict__ head, const uint8_t* __restrict__ ist,
                               const uint8_t* __restrict__ islong, unsigned long long* __restrict__ end)
@@ -326,35 +268,6 @@ __global__ void k_id_flags(const int4* __restrict__ vrec, int64_t nv, const int4
         flag[(int64_t)erec[i].x - idlo] = 1;
         flag[(int64_t)erec[i].y - idlo] = 1;
     }
-}
-
-// Exclusive scan of byte flags in blocks of kChunk: pass 1 block sums.
-__global__ void k_flag_count(const uint8_t* __restrict__ flag, int64_t n, int64_t* __restrict__ block_count)
-{
-    const int64_t i0 = (int64_t)blockIdx.x * kChunk + (int64_t)threadIdx.x * kPer;
-    int64_t c = 0;
-    for (int q = 0; q < kPer; ++q)
-        if (i0 + q < n) c += flag[i0 + q];
-    int64_t total;
-    block_exclusive_scan(c, &total);
-    if (threadIdx.x == 0) block_count[blockIdx.x] = total;
-}
-
-// Pass 2: dense rank of every present id.
-__global__ void k_flag_rank(const uint8_t* __restrict__ flag, int64_t n, const int64_t* __restrict__ block_off,
-                            int32_t* __restrict__ rank)
-{
-    const int64_t i0 = (int64_t)blockIdx.x * kChunk + (int64_t)threadIdx.x * kPer;
-    int64_t c = 0;
-    for (int q = 0; q < kPer; ++q)
-        if (i0 + q < n) c += flag[i0 + q];
-    int64_t total;
-    int64_t at = block_off[blockIdx.x] + block_exclusive_scan(c, &total);
-    for (int q = 0; q < kPer; ++q)
-        if (i0 + q < n) {
-            rank[i0 + q] = flag[i0 + q] ? (int32_t)at : -1;
-            at += flag[i0 + q];
-        }
 }
 
 __global__ void k_vertex_labels(const int4* __restrict__ vrec, int64_t nv, int32_t idlo, const int32_t* __restrict__ rank,
@@ -501,6 +414,13 @@ gspan_status load_text(gspan_ctx* ctx, const char* text, int64_t len, gspan_grap
                         "text has a token the device loader does not read like the reference's scanf-based reader "
                         "(an integer followed by other characters, an integer outside int32, or a token of 64 "
                         "characters or more); load it with the host reader");
+        }
+        if (end != ~0ull) {
+            freeall();
+            return fail(ctx, GSPAN_ERR_INVALID,
+                        "text has a record with a field that is not an integer, or cut off by the end of the text; "
+                        "the reference's reader then reuses the previous record's values: load it with the host "
+                        "reader");
         }
         const int64_t stop = end == ~0ull ? ntok : (int64_t)(end >> 1);
         k_records<<<grid_of(ntok), kThreads, 0, s>>>(d_text, d_tok, ntok, d_head, d_val, stop, d_vrec, d_erec, d_cnt,

@@ -10,6 +10,9 @@
 //   --domains auto|bitmap|hash
 //   --hash-threshold X     auto domains: hashset when 64 * size < |V| * X
 //   --device N
+//   --prune                drop vertices of labels with fewer than min_support
+//                          vertices before mining (the reference's prune_graph,
+//                          left commented out at fsm.cu:28-29); same output
 //   --stats                run statistics as one JSON object on stderr
 #include <chrono>
 #include <cstdio>
@@ -70,6 +73,8 @@ Options parse(int argc, char* argv[])
             opt.o.hash_threshold = std::atof(value().c_str());
         } else if (a == "--device") {
             opt.o.device = std::atoi(value().c_str());
+        } else if (a == "--prune") {
+            opt.o.prune = 1;
         } else {
             throw std::runtime_error("unknown option " + a);
         }
@@ -103,12 +108,13 @@ void print_stats(const gspan_stats& st)
                  "{\"seeds\": %llu, \"extended\": %llu, \"patterns\": %llu, \"support_keys\": %llu, "
                  "\"kernel_launches\": %llu, \"levels\": %d, \"mine_ms\": %.3f, \"frontier_rows\": %llu, "
                  "\"materialized_rows\": %llu, \"mask_parents\": %llu, \"candidate_parents\": %llu, "
-                 "\"h2d_bytes\": %llu, \"d2h_bytes\": %llu}\n",
+                 "\"h2d_bytes\": %llu, \"d2h_bytes\": %llu, \"pruned_vertices\": %llu, \"pruned_entries\": %llu}\n",
                  (unsigned long long)st.seeds, (unsigned long long)st.extended, (unsigned long long)st.patterns,
                  (unsigned long long)st.support_keys, (unsigned long long)st.kernel_launches, st.levels, st.mine_ms,
                  (unsigned long long)st.frontier_rows, (unsigned long long)st.materialized_rows,
                  (unsigned long long)st.mask_parents, (unsigned long long)st.candidate_parents,
-                 (unsigned long long)st.h2d_bytes, (unsigned long long)st.d2h_bytes);
+                 (unsigned long long)st.h2d_bytes, (unsigned long long)st.d2h_bytes,
+                 (unsigned long long)st.pruned_vertices, (unsigned long long)st.pruned_entries);
 }
 
 }  // namespace
@@ -117,7 +123,7 @@ int main(int argc, char* argv[])
 {
     if (argc < 4) {
         std::printf("usage: %s input_graph min_support k [--text] [--path auto|candidate|mask] "
-                    "[--domains auto|bitmap|hash] [--hash-threshold X] [--device N] [--stats]\n",
+                    "[--domains auto|bitmap|hash] [--hash-threshold X] [--device N] [--prune] [--stats]\n",
                     argv[0]);
         return 0;
     }

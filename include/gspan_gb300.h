@@ -65,6 +65,11 @@ typedef struct gspan_opts {
     double mask_bias;            /* auto path: a parent takes the mask path when its estimated candidate work
                                     exceeds mask_bias / 8 x the dense words the mask path clears.
                                     0 selects the default (1.0) */
+    int32_t prune;               /* 1: before mining a single graph, drop every vertex whose label occurs on
+                                    fewer than min_support vertices, with its edges (the reference's unused
+                                    prune_graph, graph.cc:216-266, done on the device).  Patterns and
+                                    supports are unchanged; `extended` then counts the pruned graph's
+                                    children.  Ignored for batches.  Default 0 */
 } gspan_opts;
 
 /* Run statistics.  Counts are exact and identical to those of the reference's
@@ -102,6 +107,8 @@ typedef struct gspan_stats {
     double domain_ms;            /* domain-size reductions */
     uint64_t canonical_checks;   /* children that needed the minimum-code test (host) */
     double canonical_ms;         /* host time in tests not already done while the GPU counted */
+    uint64_t pruned_vertices;    /* opts.prune: vertices dropped before mining (0 otherwise) */
+    uint64_t pruned_entries;     /* opts.prune: directed entries dropped with them */
 } gspan_stats;
 
 typedef struct gspan_ctx gspan_ctx;

@@ -5,6 +5,8 @@ import os
 import subprocess
 import tempfile
 
+import numpy as np
+
 from gspan_gb300 import datagen
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -73,3 +75,20 @@ def random_graphs():
         out.append((f"cl{seed}", datagen.chung_lu(500, 1500, 2.1, 5, 1.0, 300 + seed, max_deg=60,
                                                   nelabels=1 + seed % 2), [(20, 3), (8, 4)]))
     return out
+
+
+def numpy_prune(g, min_sup):
+    """graph.cc:216-266: keep vertices whose label has >= min_sup vertices,
+    renumber them in ascending order, keep entries between kept vertices in
+    their original order."""
+    labels, counts = np.unique(g.vlabels, return_counts=True)
+    freq = dict(zip(labels.tolist(), counts.tolist()))
+    keep = np.array([freq[int(x)] >= min_sup for x in g.vlabels], dtype=bool)
+    new_id = np.cumsum(keep) - 1
+    e = g.edges
+    ek = keep[e[:, 0]] & keep[e[:, 1]] if len(e) else np.zeros(0, bool)
+    edges = np.stack([new_id[e[ek, 0]], new_id[e[ek, 1]], e[ek, 2]], axis=1).astype(np.int32) \
+        if ek.any() else np.zeros((0, 3), np.int32)
+    deg = np.bincount(edges[:, 0], minlength=int(keep.sum())) if len(edges) else np.zeros(int(keep.sum()), int)
+    offsets = np.concatenate([[0], np.cumsum(deg)]).astype(np.int32)
+    return datagen.CSR(offsets, g.vlabels[keep].astype(np.int32), edges)

@@ -92,3 +92,53 @@ def test_missing_file_is_rejected():
     r = subprocess.run([os.path.join(ROOT, "gspan_gb300", "_lib", "fsm"), "/nonexistent.bin", "10", "2"],
                        capture_output=True, text=True)
     assert r.returncode == 1 and "failed to open file" in r.stderr
+
+
+# Malformed records: the reference's reader (graph.cc:38-64) keeps reading; a
+# failed conversion leaves that variable and the record's later ones as the
+# previous record set them, and the record is still added.
+MALFORMED = [
+    "v 0 1\nv 1 2\ne 0 1 0\nv x 3\nv 2 5\ne 1 2 0\n",
+    "v 1 2\nv 2 2\ne 1 2 0\nv abc 3\ne 1 3 0\nv 3 2\n",
+    "v 1 2\nv 2 2\ne 1 2 0\ne 1\n",
+    "v 1 2 v 2 2 e 1 2 0 e 2 - 0 e 1 1 0",
+    "v 1 2\ne 1 2 0\nv 12ab 3\ne 4 5 7\n",
+    "t # 0\nv 1 2\ne 1 2 3\ne 4 x\nv 9\n",
+    "t # x\nv 1 2\n",
+    "v 1 2\ne 1 2 0\ne 7 -\n",
+]
+
+
+@pytest.mark.parametrize("text", MALFORMED)
+def test_convert_reads_malformed_records_like_the_reference(text, tmp_path):
+    src = tmp_path / "g.txt"
+    src.write_text(text)
+    out = tmp_path / "g.bin"
+    r = subprocess.run([CONVERT, str(src), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    if os.path.exists(REF_CONVERT):
+        ref_out = tmp_path / "ref.bin"
+        rr = subprocess.run([REF_CONVERT, str(src), str(ref_out)], capture_output=True, text=True, check=True)
+        assert rr.stdout == r.stdout
+        assert ref_out.read_bytes() == out.read_bytes()
+
+
+def test_convert_stale_values_by_hand(tmp_path):
+    """'v x 3' fails at its id: the reference still adds vertex v with the values
+    the previous record ('e 0 1 0') left, id 1 and label 0, relabelling vertex
+    1; 'x' and '3' are then skipped as record heads."""
+    src = tmp_path / "g.txt"
+    src.write_text("v 0 1\nv 1 2\ne 0 1 0\nv x 3\nv 2 5\ne 1 2 0\n")
+    out = tmp_path / "g.bin"
+    subprocess.run([CONVERT, str(src), str(out)], capture_output=True, check=True)
+    g = datagen.load_bin(str(out))
+    assert g.vlabels.tolist() == [1, 0, 5] and g.m == 4
+
+
+@pytest.mark.parametrize("text", ["v 1\n", "t # 5\ne x\n", "e 1 2\n"])
+def test_convert_refuses_values_never_assigned(text, tmp_path):
+    """The reference would read an uninitialised variable here (undefined)."""
+    src = tmp_path / "g.txt"
+    src.write_text(text)
+    r = subprocess.run([CONVERT, str(src), str(tmp_path / "g.bin")], capture_output=True, text=True)
+    assert r.returncode != 0 and "malformed record" in r.stderr
