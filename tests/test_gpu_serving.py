@@ -1,8 +1,10 @@
 """Serving: jobs submitted while others run overlap on the GPU; every result
-must be the same alone and in the mix."""
+must be the same alone and in the mix, and equal to the CPU oracle's."""
 import random
 
 import pytest
+
+from helpers import lines_of, run_port
 
 pytestmark = pytest.mark.gpu
 
@@ -34,6 +36,17 @@ def test_results_same_alone_and_in_mix(slots, budget):
     for (got, info), want in zip(mixed, alone):
         assert got == want
         assert info["status"] == 0 and info["latency_ms"] >= info["run_ms"] >= 0
+    # Served results against the oracle, one job per graph of the pool (the
+    # oracle's 3-edge jobs on the 20,000-vertex graphs take seconds).
+    checked = set()
+    for (got, info), (gi, k, sup) in zip(mixed, jobs):
+        if gi in checked:
+            continue
+        checked.add(gi)
+        lines, st = run_port(graphs[gi], sup, k, with_stats=True, stream_last=True)
+        assert lines_of(got) == lines, (gi, k, sup)
+        assert info["stats"]["extended"] == st["extended"], (gi, k, sup)
+    assert len(checked) >= 4
 
 
 def test_bad_requests():
