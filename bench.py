@@ -99,6 +99,12 @@ def workloads():
         "chung_lu_3_7m_k4": dict(
             make=lambda: datagen.chung_lu_3_7m(3), min_support=100000, k=4, cpu=False,
             desc="Chung-Lu 3,700,000 V / 16,500,000 E (as chung_lu_3_7m), min support 100,000, 4 edges"),
+        # The large graph at four edges and its stated support: the 3-edge
+        # level (about 1e12 embeddings) is generated inside the 4-edge row
+        # pass, never stored.
+        "chung_lu_3_7m_k4_s20k": dict(
+            make=lambda: datagen.chung_lu_3_7m(3), min_support=20000, k=4, cpu=False,
+            desc="Chung-Lu 3,700,000 V / 16,500,000 E (as chung_lu_3_7m), min support 20,000, 4 edges"),
         # A wide label space: 100 vertex labels x 3 edge labels = 300 tuple keys
         # (the row pass's 16-word build).
         "chung_lu_100k_wide": dict(
@@ -322,7 +328,7 @@ def gpu_arm(args, wl) -> None:
             g.save(path)
             cpu = cpu_sample(path, wl, host_cores())
 
-    with Miner(device=local, profile=True) as m:
+    with Miner(device=local, profile=True, fused_last=args.fused_last, prune=args.prune) as m:
         with ClockSampler(local, settle_s=1.0) as clk:
             # The clock sampler starts before the warm-up, so its start-up does not
             # land on a timed step; it samples through the timed region.
@@ -390,7 +396,8 @@ def gpu_arm(args, wl) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
         "config": {"workload": args.workload, "description": wl["desc"], "min_support": sup, "k": k,
                    "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
-                   "engine": "plain (level-synchronous)"},
+                   "engine": "plain (level-synchronous)", "fused_last": ["auto", "off", "always"][args.fused_last],
+                   "prune": bool(args.prune)},
         "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_total / len(e2e_ms),
                 "h2d_bytes_per_step": int(h2d_graph + stats[-1]["h2d_bytes"]),
                 "d2h_bytes_per_step": int(statistics.median(e2e_d2h))},
@@ -411,6 +418,8 @@ def gpu_arm(args, wl) -> None:
                                "seed": sum(s["seed_ms"] for s in stats) / len(stats),
                                "domain sizes": sum(s["domain_ms"] for s in stats) / len(stats)},
         "paths": {"mask_parents": stats[-1]["mask_parents"], "candidate_parents": stats[-1]["candidate_parents"]},
+        "fused_rows_per_step": stats[-1]["fused_rows"],
+        "pruned": {"vertices": stats[-1]["pruned_vertices"], "entries": stats[-1]["pruned_entries"]},
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -620,6 +629,9 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", default="chung_lu_100k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fused-last", type=int, default=0, choices=[0, 1, 2],
+                    help="next-to-last level: 0 auto, 1 stored, 2 generated inside the last row pass")
+    ap.add_argument("--prune", action="store_true", help="drop vertices of infrequent labels before mining")
     ap.add_argument("--slots", type=int, default=4, help="serving: concurrent contexts")
     ap.add_argument("--serving-jobs", type=int, default=100, help="serving: jobs per stream (one step)")
     ap.add_argument("--rate", type=float, default=50.0, help="serving: mean arrivals per second (0: all at once)")

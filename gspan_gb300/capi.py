@@ -47,7 +47,7 @@ class Opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("domain_mode", ctypes.c_int32),
                 ("hash_threshold", ctypes.c_double), ("mem_fraction", ctypes.c_double),
                 ("profile", ctypes.c_int32), ("path", ctypes.c_int32), ("mask_bias", ctypes.c_double),
-                ("prune", ctypes.c_int32)]
+                ("prune", ctypes.c_int32), ("fused_last", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -66,7 +66,8 @@ class Stats(ctypes.Structure):
                 ("materialize_bytes", ctypes.c_double),
                 ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double),
                 ("canonical_checks", ctypes.c_uint64), ("canonical_ms", ctypes.c_double),
-                ("pruned_vertices", ctypes.c_uint64), ("pruned_entries", ctypes.c_uint64)]
+                ("pruned_vertices", ctypes.c_uint64), ("pruned_entries", ctypes.c_uint64),
+                ("fused_rows", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -241,7 +242,7 @@ class Miner:
 
     def __init__(self, device: int = 0, domain_mode: int = 0, hash_threshold: float = 1.0,
                  profile: bool = False, mem_fraction: float = 0.85, path: int = 0, mask_bias: float = 1.0,
-                 prune: bool = False):
+                 prune: bool = False, fused_last: int = 0):
         opts = Opts()
         _lib.gspan_opts_default(ctypes.byref(opts))
         opts.device = device
@@ -252,6 +253,7 @@ class Miner:
         opts.path = path
         opts.mask_bias = mask_bias
         opts.prune = 1 if prune else 0
+        opts.fused_last = fused_last
         self._ctx = ctypes.c_void_p()
         rc = _lib.gspan_ctx_create(ctypes.byref(opts), ctypes.byref(self._ctx))
         if rc != GSPAN_OK:
@@ -360,7 +362,7 @@ class Miner:
             col.close()
         return (flat if raw else decode_results(flat, ninst)), st.as_dict()
 
-    TUNABLES = ("domain_mode", "hash_threshold", "mem_fraction", "path", "mask_bias")
+    TUNABLES = ("domain_mode", "hash_threshold", "mem_fraction", "path", "mask_bias", "fused_last")
 
     def autotune(self, dg: DeviceGraph, k: int, min_supports, candidates=None, ncand: int = 6, repeats: int = 2):
         """Times the job under each option set (dicts of TUNABLES; None: the

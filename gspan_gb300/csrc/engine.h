@@ -183,6 +183,16 @@ struct ParentMeta {
     int64_t b_off;              // MB: nv x n x bw words
     int64_t sz_off;             // domain sizes: nsrc*K*(nv+1) forward, then nback*nel*nv backward
     uint32_t range[kMaxV][kMaxMaskWords];   // per source: keys inside its valid range
+    // Two-level last step (k_mask_gen): this parent's rows are not in a table
+    // but generated from the rows of its own parent gen_p2 (one level up) as
+    // that parent's child tuple: forward (gen_kind 1) from source gen_s with
+    // window key gen_kc, or backward (gen_kind 2) to target gen_s with edge
+    // label gen_kc.  gen_kind 0: rows come from the level table.  tile_begin
+    // then counts 32-row tiles of gen_p2's rows.
+    int32_t gen_p2;
+    int16_t gen_kind;
+    int16_t gen_s;
+    int32_t gen_kc;
 };
 
 // Per-level key space arrays on the device.
@@ -266,6 +276,12 @@ struct MaskArgs {
     unsigned long long* tile_counter;
     unsigned long long* scanned; // adjacency entries read by the sweep
     uint32_t* status;
+    // Two-level last step only: the parents' own parents (one level up), the
+    // table of their rows and its first entry column (-1 if none).
+    const ParentMeta* gen_parents = nullptr;
+    int32_t* const* gen_cols = nullptr;
+    int32_t gen_ecol = -1;
+    int32_t gen_nv = 0;          // most vertices of any generated row
 };
 // Segment masks (zeroed by the caller), singleton masks and, when
 // allocated, segment starts, in one pass over each vertex's entries.
@@ -276,6 +292,9 @@ cudaError_t launch_segments(DevGraph& g, cudaStream_t st);
 // and kFlagSelfLoop.
 cudaError_t launch_entry_flags(DevGraph& g, uint32_t* status, cudaStream_t st);
 cudaError_t launch_mask_rows(const MaskArgs& a, cudaStream_t st);
+// Two-level last step: the row pass over rows generated from gen_parents'
+// rows (every parent has gen_kind != 0), none of them stored.
+cudaError_t launch_mask_gen(const MaskArgs& a, cudaStream_t st);
 // Prefix of the touched lists, then the sweep (two launches).
 cudaError_t launch_mask_sweep(const MaskArgs& a, cudaStream_t st);
 

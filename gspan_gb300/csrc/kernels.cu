@@ -761,6 +761,10 @@ struct MaskDev {
     unsigned long long* tile_counter;
     unsigned long long* scanned;
     uint32_t* status;
+    const ParentMeta* gen_parents;
+    int32_t* const* gen_cols;
+    int32_t gen_ecol;
+    int32_t gen_vs, gen_es;      // shared-memory strides of generated rows (odd)
 };
 
 // OR `bits` into *p and return the bits that were not set before (a word
@@ -889,9 +893,309 @@ __device__ __forceinline__ int32_t find_parent_tile(const ParentMeta* parents, i
     return lo;
 }
 
-// Row pass: lane per row.  Updates R (listing new source images), H and M for
-// every source, and counts and MB masks for backward tuples (at most one per
-// row and rightmost-path target).
+// Entry column j (the adjacency index of pattern edge j's image) of the lane's
+// row: from the level table ...
+struct EcolFromTable {
+    int32_t* const* cols;
+    int32_t base;
+    int64_t row;
+    __device__ __forceinline__ int32_t operator()(int j) const { return __ldg(cols[base + j] + row); }
+};
+
+// ... or from a row generated in shared memory (two-level last step).
+struct EcolFromShared {
+    const int32_t* e;
+    __device__ __forceinline__ int32_t operator()(int j) const { return e[j]; }
+};
+
+// The row pass's work for one row per lane of parent P: updates R (listing new
+// source images), H and M for every source, and counts and MB masks for
+// backward tuples (at most one per row and rightmost-path target).  `img` holds
+// the lane's row images; lanes with !live take part in the warp-wide steps only.
+template <int MW, class Ecol>
+__device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, const int32_t* img, const Ecol& ecol,
+                                         bool live, int lane)
+{
+    const int32_t K = a.nel * a.lwin;
+    const int mw = a.mw;
+    const int nv = P.nv, nsrc = P.nsrc;
+    const int min_label = P.min_label;
+    for (int s = 0; s < nsrc; ++s) {
+        const int32_t u = live ? img[P.src_v[s]] : -1;
+        const unsigned lm = __ballot_sync(kFull, live);
+        bool first_row = false;   // this lane's group made R[u] non-zero
+        if (live) {
+            const unsigned peers = __match_any_sync(lm, u);
+            if (lane == __ffs(peers) - 1)
+                first_row = atomicAdd(a.R + P.r_off + (int64_t)s * P.nloc + (u - P.vbase), (uint32_t)__popc(peers)) == 0;
+        }
+        // One append per warp for the source images seen for the first time.
+        const unsigned fm = __ballot_sync(kFull, first_row);
+        if (fm) {
+            const int first = __ffs(fm) - 1;
+            uint32_t base = 0;
+            if (lane == first) base = atomicAdd(a.tcount + P.ps_begin + s, (uint32_t)__popc(fm));
+            base = __shfl_sync(kFull, base, first);
+            if (first_row) {
+                const uint32_t slot = base + __popc(fm & lanemask_lt());
+                if (slot < (uint32_t)P.t_cap)
+                    a.touched[P.t_off + (int64_t)s * P.t_cap + slot] = u;
+                else
+                    atomicOr(a.status, kErrCursor);
+            }
+        }
+        uint32_t mk[MW] = {};
+        if (live) {
+        const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
+        const uint64_t lo = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
+                                   : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
+        // H of this source, indexed by batch-wide entry index.
+        uint32_t* Hs = a.H + P.h_off + (int64_t)s * P.mloc - P.ebase;
+        uint32_t ex[MW] = {};
+        if (a.ecol >= 0) {
+            // One edge label.  Images joined to the source by a pattern
+            // edge are found through the row's entry columns (or their
+            // reverse entries); the others through the edge index (or by
+            // search, after a cheap existence test from the shorter side).
+            // Vertices are visited in label order, so each label's hits
+            // are summed on the fly: a segment is lost to the row when
+            // its images fill all of it.
+            const int vs = P.src_v[s];
+            int cur_t = -1, gstart = 0;
+            int32_t hits = 0, minlb = e, maxub = b;
+            for (int oi = 0; oi <= nv; ++oi) {
+                const int j = oi < nv ? P.lorder[oi] : 0;
+                const int t = oi < nv ? P.vlab[j] : -1;
+                if (t != cur_t) {
+                    if (hits > 0) {
+                        const uint32_t kc = (uint32_t)(cur_t - P.lbase);
+                        bool lost;
+                        if (hits == 1) {
+                            // One hit fills its segment only when the segment has one entry.
+                            lost = (__ldg(a.segone + (int64_t)u * mw + (kc >> 5)) >> (kc & 31u)) & 1u;
+                        } else {
+                            const uint32_t segk = (uint32_t)(pack_entry(0, (uint32_t)cur_t, 0) >> 32);
+                            const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
+                            const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
+                            lost = first && last && maxub - minlb == hits;
+                        }
+                        if (lost) {
+#pragma unroll
+                            for (int w = 0; w < MW; ++w)
+                                ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
+                        }
+                    }
+                    cur_t = t;
+                    gstart = oi;
+                    hits = 0;
+                    minlb = e;
+                    maxub = b;
+                }
+                if (oi == nv) break;
+                const uint64_t seg0 = pack_entry(0, (uint32_t)t, 0);
+                if (t < min_label || seg0 < lo) continue;
+                const int32_t x = img[j];
+                if (a.loops) {
+                    // Images may repeat: one hit per distinct image (equal
+                    // images have equal labels, so within the group).
+                    bool dup = false;
+                    for (int q = gstart; q < oi; ++q) dup |= img[P.lorder[q]] == x;
+                    if (dup) continue;
+                } else if (j == vs) {
+                    continue;   // no self-loops: the source is not its own neighbour
+                }
+                const uint64_t key = seg0 | (uint32_t)x;
+                const int jj = P.pair_edge[s][j];
+                int32_t pos = -1;
+                if (jj >= 0) {
+                    const int32_t stored = ecol(jj);
+                    pos = P.e_from[jj] == vs ? stored : __ldg(a.rev + stored);
+                    // The entry column holds the image edge's entry (or, from its
+                    // other end, the reverse entry): inside u's list it is the key.
+                    if (pos < b || pos >= e) pos = -1;
+                }
+                if (pos < 0) {
+                    if (x == u && !((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
+                    if (a.eidx) {
+                        pos = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)u, key);
+                        if (pos < 0) continue;
+                    } else {
+                        if (x != u && jj < 0 && a.symmetric) {
+                            const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
+                            if (4 * (xe - xb) < e - b) {
+                                const uint64_t rk = pack_entry(0, (uint32_t)P.vlab[vs], (uint32_t)u);
+                                const int32_t rp = lower_bound_entry(a.adj, xb, xe, rk);
+                                if (rp >= xe || __ldg(a.adj + rp) != rk) continue;
+                            }
+                        }
+                        pos = lower_bound_entry(a.adj, b, e, key);
+                        if (pos >= e || __ldg(a.adj + pos) != key) continue;
+                    }
+                }
+                int32_t lb = pos, ub = pos + 1;
+                if (a.parallel) {
+                    while (lb > b && __ldg(a.adj + lb - 1) == key) --lb;
+                    while (ub < e && __ldg(a.adj + ub) == key) ++ub;
+                }
+                for (int32_t q = lb; q < ub; ++q) atomicAdd(Hs + q, 1u);
+                hits += ub - lb;
+                minlb = min(minlb, lb);
+                maxub = max(maxub, ub);
+            }
+        } else
+        for (int el = 0; el < a.nel; ++el) {
+            for (int i = 0; i < nv; ++i) {
+                const int t = P.vlab[i];
+                const uint64_t seg0 = pack_entry((uint32_t)el, (uint32_t)t, 0);
+                if (t < min_label || seg0 < lo) continue;
+                bool lead = true;   // first pattern vertex of this label handles the label group
+                for (int q = 0; q < i; ++q) lead &= P.vlab[q] != t;
+                if (!lead) continue;
+                int32_t hits = 0, minlb = e, maxub = b;
+                for (int j = i; j < nv; ++j) {
+                    if (P.vlab[j] != t) continue;
+                    const int32_t x = img[j];
+                    if (a.loops) {
+                        bool dup = false;
+                        for (int q = i; q < j; ++q) dup |= img[q] == x;
+                        if (dup) continue;
+                    }
+                    // Most image pairs are not adjacent.  A vertex reaches
+                    // itself only through a self-loop; a pair that the
+                    // pattern does not join is first looked up from the
+                    // shorter side when the graph is symmetric.
+                    if (x == u) {
+                        if (!((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
+                    } else if (!a.eidx && a.symmetric && !((P.src_adj[s] >> j) & 1)) {
+                        const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
+                        if (4 * (xe - xb) < e - b) {
+                            const uint64_t rk = pack_entry((uint32_t)el, (uint32_t)P.vlab[P.src_v[s]], (uint32_t)u);
+                            const int32_t rp = lower_bound_entry(a.adj, xb, xe, rk);
+                            if (rp >= xe || __ldg(a.adj + rp) != rk) continue;
+                        }
+                    }
+                    const uint64_t key = seg0 | (uint32_t)x;
+                    int32_t lb;
+                    if (a.eidx) {
+                        lb = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)u, key);
+                        if (lb < 0) continue;
+                    } else {
+                        lb = lower_bound_entry(a.adj, b, e, key);
+                    }
+                    int32_t ub = lb;
+                    while (ub < e && __ldg(a.adj + ub) == key) {
+                        atomicAdd(Hs + ub, 1u);
+                        ++ub;
+                    }
+                    if (ub > lb) {
+                        hits += ub - lb;
+                        minlb = min(minlb, lb);
+                        maxub = max(maxub, ub);
+                    }
+                }
+                if (hits > 0) {
+                    // The row has no child in this segment when its images fill all of it.
+                    const uint32_t segk = (uint32_t)(seg0 >> 32);
+                    const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
+                    const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
+                    if (first && last && maxub - minlb == hits) {
+                        const uint32_t kc = (uint32_t)(el * a.lwin + t - P.lbase);
+#pragma unroll
+                        for (int w = 0; w < MW; ++w)
+                            ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < MW; ++w)
+            mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
+        }
+        if (mw == 1 && nv <= kMaskBatch) {
+            // One mask word per vertex: read every vertex's word first, so
+            // the L2 round trips overlap, then OR where bits are missing.
+            uint32_t* const mrow = a.M + P.m_off + (int64_t)s * (nv + 1) * P.nloc;
+            uint32_t cur[kMaskBatch];
+#pragma unroll
+            for (int p = 0; p < kMaskBatch; ++p)
+                cur[p] = p < nv && mk[0] ? __ldcg(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase)) : ~0u;
+#pragma unroll
+            for (int p = 0; p < kMaskBatch; ++p) {
+                if (p >= nv) break;
+                const uint32_t fresh =
+                    (mk[0] & ~cur[p]) ? mk[0] & ~atomicOr(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase), mk[0]) : 0u;
+                add_fresh_bits(fresh, a.sizes, P.sz_off + (int64_t)s * K * (nv + 1) + p, nv + 1, 0, lane);
+            }
+        } else {
+            for (int p = 0; p < nv; ++p) {
+                uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * P.nloc + (live ? img[p] - P.vbase : 0)) * mw;
+                const int64_t out = P.sz_off + (int64_t)s * K * (nv + 1) + p;
+                for (int w = 0; w < mw; ++w) add_fresh_bits(or_fresh(rowm + w, mk[w]), a.sizes, out, nv + 1, w, lane);
+            }
+        }
+    }
+
+    for (int t = 0; t < P.nback; ++t) {
+        bool ok = false;
+        int32_t bel = 0;
+        if (live) {
+            const int bv = P.back_v[t];
+            const int32_t x = img[bv];
+            const int32_t un = img[P.vn];
+            const uint32_t tlx = (uint32_t)P.vlab[bv];
+            const int32_t b = __ldg(a.offsets + un), e = __ldg(a.offsets + un + 1);
+            for (int32_t el = P.back_eq[t] ? P.back_el[t] : P.back_el[t] + 1; el < a.nel && !ok; ++el) {
+                const uint64_t want = pack_entry((uint32_t)el, tlx, (uint32_t)x);
+                int32_t pos;
+                if (a.eidx) {
+                    pos = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)un, want);
+                } else {
+                    pos = lower_bound_entry(a.adj, b, e, want);
+                    if (pos >= e || __ldg(a.adj + pos) != want) pos = -1;
+                }
+                if (pos >= 0) {
+                    // has_edge: the row already uses an edge (un, x, el).
+                    // Without self-loops images are distinct, so that is
+                    // a code edge joining v_n and the target.
+                    bool used = false;
+                    if (!a.loops && el < 32) {
+                        used = (P.back_used[t] >> el) & 1u;
+                    } else {
+                        for (int j = 0; j < P.nedge; ++j) {
+                            if (P.e_el[j] != el) continue;
+                            const int32_t f = img[P.e_from[j]], g2 = img[P.e_to[j]];
+                            if ((f == un && g2 == x) || (g2 == un && f == x)) used = true;
+                        }
+                    }
+                    if (!used) {
+                        ok = true;
+                        bel = el;
+                    }
+                }
+            }
+        }
+        const int32_t bk = t * a.nel + bel;
+        const int32_t key = P.key_base + nsrc * K + bk;
+        const unsigned mask = __ballot_sync(kFull, ok);
+        if (ok) {
+            const unsigned peers = __match_any_sync(mask, key);
+            if (lane == __ffs(peers) - 1) atomicAdd(a.counts + key, (unsigned long long)__popc(peers));
+        }
+        if (mask) {
+            const int64_t out = P.sz_off + (int64_t)nsrc * K * (nv + 1);
+            for (int p = 0; p < nv; ++p) {
+                const uint32_t got =
+                    ok ? or_fresh(a.MB + P.b_off + ((int64_t)p * P.nloc + (img[p] - P.vbase)) * P.bw + (bk >> 5),
+                                  1u << (bk & 31))
+                       : 0u;
+                for (int w = 0; w < P.bw; ++w)
+                    add_fresh_bits((bk >> 5) == w ? got : 0u, a.sizes, out + p, nv, w, lane);
+            }
+        }
+    }
+}
+
+// Row pass: lane per row of the level table.
 template <int MW>
 __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 2) k_mask_rows(MaskDev a)
 {
@@ -899,8 +1203,6 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 
     int32_t (*img_all)[kMaxV + 1] = img_s[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     int32_t* img = img_all[lane];
-    const int32_t K = a.nel * a.lwin;
-    const int mw = a.mw;
 
     for (;;) {
         long long tile = 0;
@@ -908,237 +1210,70 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 
         tile = __shfl_sync(kFull, tile, 0);
         if (tile >= a.ntiles) break;
         const ParentMeta& P = a.parents[find_parent_tile(a.parents, a.nparents, tile)];
-        const int nv = P.nv, nsrc = P.nsrc;
-        const int min_label = P.min_label;
+        const int nv = P.nv;
         const int64_t row = P.row_begin + (tile - P.tile_begin) * 32 + lane;
         const bool live = row < P.row_end;
         for (int p = 0; p < nv; ++p) img[p] = live ? __ldcs(a.in_cols[p] + row) : -1;
+        mask_row<MW>(a, P, img, EcolFromTable{a.in_cols, a.ecol, row}, live, lane);
+        __syncwarp();
+    }
+}
 
-        for (int s = 0; s < nsrc; ++s) {
-            const int32_t u = live ? img[P.src_v[s]] : -1;
-            const unsigned lm = __ballot_sync(kFull, live);
-            bool first_row = false;   // this lane's group made R[u] non-zero
-            if (live) {
-                const unsigned peers = __match_any_sync(lm, u);
-                if (lane == __ffs(peers) - 1)
-                    first_row = atomicAdd(a.R + P.r_off + (int64_t)s * P.nloc + (u - P.vbase), (uint32_t)__popc(peers)) == 0;
-            }
-            // One append per warp for the source images seen for the first time.
-            const unsigned fm = __ballot_sync(kFull, first_row);
-            if (fm) {
-                const int first = __ffs(fm) - 1;
-                uint32_t base = 0;
-                if (lane == first) base = atomicAdd(a.tcount + P.ps_begin + s, (uint32_t)__popc(fm));
-                base = __shfl_sync(kFull, base, first);
-                if (first_row) {
-                    const uint32_t slot = base + __popc(fm & lanemask_lt());
-                    if (slot < (uint32_t)P.t_cap)
-                        a.touched[P.t_off + (int64_t)s * P.t_cap + slot] = u;
-                    else
-                        atomicOr(a.status, kErrCursor);
-                }
-            }
-            uint32_t mk[MW] = {};
-            if (live) {
-            const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
-            const uint64_t lo = s == 0 ? pack_entry(0, (uint32_t)min_label, 0)
-                                       : pack_entry((uint32_t)P.src_el[s], (uint32_t)P.src_tl[s], 0);
-            // H of this source, indexed by batch-wide entry index.
-            uint32_t* Hs = a.H + P.h_off + (int64_t)s * P.mloc - P.ebase;
-            uint32_t ex[MW] = {};
-            if (a.ecol >= 0) {
-                // One edge label.  Images joined to the source by a pattern
-                // edge are found through the row's entry columns (or their
-                // reverse entries); the others through the edge index (or by
-                // search, after a cheap existence test from the shorter side).
-                // Vertices are visited in label order, so each label's hits
-                // are summed on the fly: a segment is lost to the row when
-                // its images fill all of it.
-                const int vs = P.src_v[s];
-                int cur_t = -1, gstart = 0;
-                int32_t hits = 0, minlb = e, maxub = b;
-                for (int oi = 0; oi <= nv; ++oi) {
-                    const int j = oi < nv ? P.lorder[oi] : 0;
-                    const int t = oi < nv ? P.vlab[j] : -1;
-                    if (t != cur_t) {
-                        if (hits > 0) {
-                            const uint32_t kc = (uint32_t)(cur_t - P.lbase);
-                            bool lost;
-                            if (hits == 1) {
-                                // One hit fills its segment only when the segment has one entry.
-                                lost = (__ldg(a.segone + (int64_t)u * mw + (kc >> 5)) >> (kc & 31u)) & 1u;
-                            } else {
-                                const uint32_t segk = (uint32_t)(pack_entry(0, (uint32_t)cur_t, 0) >> 32);
-                                const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
-                                const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
-                                lost = first && last && maxub - minlb == hits;
-                            }
-                            if (lost) {
-#pragma unroll
-                                for (int w = 0; w < MW; ++w)
-                                    ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
-                            }
-                        }
-                        cur_t = t;
-                        gstart = oi;
-                        hits = 0;
-                        minlb = e;
-                        maxub = b;
-                    }
-                    if (oi == nv) break;
-                    const uint64_t seg0 = pack_entry(0, (uint32_t)t, 0);
-                    if (t < min_label || seg0 < lo) continue;
-                    const int32_t x = img[j];
-                    if (a.loops) {
-                        // Images may repeat: one hit per distinct image (equal
-                        // images have equal labels, so within the group).
-                        bool dup = false;
-                        for (int q = gstart; q < oi; ++q) dup |= img[P.lorder[q]] == x;
-                        if (dup) continue;
-                    } else if (j == vs) {
-                        continue;   // no self-loops: the source is not its own neighbour
-                    }
-                    const uint64_t key = seg0 | (uint32_t)x;
-                    const int jj = P.pair_edge[s][j];
-                    int32_t pos = -1;
-                    if (jj >= 0) {
-                        const int32_t stored = __ldg(a.in_cols[a.ecol + jj] + row);
-                        pos = P.e_from[jj] == vs ? stored : __ldg(a.rev + stored);
-                        // The entry column holds the image edge's entry (or, from its
-                        // other end, the reverse entry): inside u's list it is the key.
-                        if (pos < b || pos >= e) pos = -1;
-                    }
-                    if (pos < 0) {
-                        if (x == u && !((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
-                        if (a.eidx) {
-                            pos = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)u, key);
-                            if (pos < 0) continue;
-                        } else {
-                            if (x != u && jj < 0 && a.symmetric) {
-                                const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
-                                if (4 * (xe - xb) < e - b) {
-                                    const uint64_t rk = pack_entry(0, (uint32_t)P.vlab[vs], (uint32_t)u);
-                                    const int32_t rp = lower_bound_entry(a.adj, xb, xe, rk);
-                                    if (rp >= xe || __ldg(a.adj + rp) != rk) continue;
-                                }
-                            }
-                            pos = lower_bound_entry(a.adj, b, e, key);
-                            if (pos >= e || __ldg(a.adj + pos) != key) continue;
-                        }
-                    }
-                    int32_t lb = pos, ub = pos + 1;
-                    if (a.parallel) {
-                        while (lb > b && __ldg(a.adj + lb - 1) == key) --lb;
-                        while (ub < e && __ldg(a.adj + ub) == key) ++ub;
-                    }
-                    for (int32_t q = lb; q < ub; ++q) atomicAdd(Hs + q, 1u);
-                    hits += ub - lb;
-                    minlb = min(minlb, lb);
-                    maxub = max(maxub, ub);
-                }
-            } else
-            for (int el = 0; el < a.nel; ++el) {
-                for (int i = 0; i < nv; ++i) {
-                    const int t = P.vlab[i];
-                    const uint64_t seg0 = pack_entry((uint32_t)el, (uint32_t)t, 0);
-                    if (t < min_label || seg0 < lo) continue;
-                    bool lead = true;   // first pattern vertex of this label handles the label group
-                    for (int q = 0; q < i; ++q) lead &= P.vlab[q] != t;
-                    if (!lead) continue;
-                    int32_t hits = 0, minlb = e, maxub = b;
-                    for (int j = i; j < nv; ++j) {
-                        if (P.vlab[j] != t) continue;
-                        const int32_t x = img[j];
-                        if (a.loops) {
-                            bool dup = false;
-                            for (int q = i; q < j; ++q) dup |= img[q] == x;
-                            if (dup) continue;
-                        }
-                        // Most image pairs are not adjacent.  A vertex reaches
-                        // itself only through a self-loop; a pair that the
-                        // pattern does not join is first looked up from the
-                        // shorter side when the graph is symmetric.
-                        if (x == u) {
-                            if (!((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
-                        } else if (!a.eidx && a.symmetric && !((P.src_adj[s] >> j) & 1)) {
-                            const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
-                            if (4 * (xe - xb) < e - b) {
-                                const uint64_t rk = pack_entry((uint32_t)el, (uint32_t)P.vlab[P.src_v[s]], (uint32_t)u);
-                                const int32_t rp = lower_bound_entry(a.adj, xb, xe, rk);
-                                if (rp >= xe || __ldg(a.adj + rp) != rk) continue;
-                            }
-                        }
-                        const uint64_t key = seg0 | (uint32_t)x;
-                        int32_t lb;
-                        if (a.eidx) {
-                            lb = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)u, key);
-                            if (lb < 0) continue;
-                        } else {
-                            lb = lower_bound_entry(a.adj, b, e, key);
-                        }
-                        int32_t ub = lb;
-                        while (ub < e && __ldg(a.adj + ub) == key) {
-                            atomicAdd(Hs + ub, 1u);
-                            ++ub;
-                        }
-                        if (ub > lb) {
-                            hits += ub - lb;
-                            minlb = min(minlb, lb);
-                            maxub = max(maxub, ub);
-                        }
-                    }
-                    if (hits > 0) {
-                        // The row has no child in this segment when its images fill all of it.
-                        const uint32_t segk = (uint32_t)(seg0 >> 32);
-                        const bool first = minlb == b || (uint32_t)(__ldg(a.adj + minlb - 1) >> 32) != segk;
-                        const bool last = maxub == e || (uint32_t)(__ldg(a.adj + maxub) >> 32) != segk;
-                        if (first && last && maxub - minlb == hits) {
-                            const uint32_t kc = (uint32_t)(el * a.lwin + t - P.lbase);
-#pragma unroll
-                            for (int w = 0; w < MW; ++w)
-                                ex[w] |= (uint32_t)(w == (int)(kc >> 5)) << (kc & 31u);
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int w = 0; w < MW; ++w)
-                mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
-            }
-            if (mw == 1 && nv <= kMaskBatch) {
-                // One mask word per vertex: read every vertex's word first, so
-                // the L2 round trips overlap, then OR where bits are missing.
-                uint32_t* const mrow = a.M + P.m_off + (int64_t)s * (nv + 1) * P.nloc;
-                uint32_t cur[kMaskBatch];
-#pragma unroll
-                for (int p = 0; p < kMaskBatch; ++p)
-                    cur[p] = p < nv && mk[0] ? __ldcg(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase)) : ~0u;
-#pragma unroll
-                for (int p = 0; p < kMaskBatch; ++p) {
-                    if (p >= nv) break;
-                    const uint32_t fresh =
-                        (mk[0] & ~cur[p]) ? mk[0] & ~atomicOr(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase), mk[0]) : 0u;
-                    add_fresh_bits(fresh, a.sizes, P.sz_off + (int64_t)s * K * (nv + 1) + p, nv + 1, 0, lane);
-                }
-            } else {
-                for (int p = 0; p < nv; ++p) {
-                    uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * P.nloc + (live ? img[p] - P.vbase : 0)) * mw;
-                    const int64_t out = P.sz_off + (int64_t)s * K * (nv + 1) + p;
-                    for (int w = 0; w < mw; ++w) add_fresh_bits(or_fresh(rowm + w, mk[w]), a.sizes, out, nv + 1, w, lane);
-                }
-            }
-        }
+// Two-level last step: warp per tile of 32 rows of a parent's own parent Q
+// (one level up).  The parent F is Q's child tuple; its rows are generated here
+// exactly as the Materialize pass of k_expand would write them - a forward
+// tuple's rows are the entries of the tuple's segment of the source image
+// that are not images of the Q row, a backward tuple's the Q rows whose first
+// valid closing edge (gspan.cu:428-445) has the tuple's label - and go through
+// mask_row in batches of 32, one per lane, never stored.
+//
+// Per-warp dynamic shared memory (ints): Q images [32][vs], Q entry columns
+// [32][es], generated images [32][vs], generated entry columns [32][es],
+// segment start, length and exclusive prefix [32] each.
+__host__ __device__ inline int gen_warp_ints(int vs, int es) { return 32 * (2 * vs + 2 * es + 3); }
 
-        for (int t = 0; t < P.nback; ++t) {
+template <int MW>
+__global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 4 : 2) k_mask_gen(MaskDev a)
+{
+    extern __shared__ __align__(16) int32_t gen_smem[];
+    const int lane = threadIdx.x & 31;
+    const int vs = a.gen_vs, es = a.gen_es;
+    int32_t* const qimg = gen_smem + (threadIdx.x >> 5) * gen_warp_ints(vs, es);
+    int32_t* const qec = qimg + 32 * vs;
+    int32_t* const gimg = qec + 32 * es;
+    int32_t* const gec = gimg + 32 * vs;
+    int32_t* const wst = gec + 32 * es;
+    int32_t* const wcnt = wst + 32;
+    int32_t* const wpre = wcnt + 32;
+    const bool ecols = a.gen_ecol >= 0;
+
+    for (;;) {
+        long long tile = 0;
+        if (lane == 0) tile = (long long)atomicAdd(a.tile_counter, 1ull);
+        tile = __shfl_sync(kFull, tile, 0);
+        if (tile >= a.ntiles) break;
+        const ParentMeta& F = a.parents[find_parent_tile(a.parents, a.nparents, tile)];
+        const ParentMeta& Q = a.gen_parents[F.gen_p2];
+        const int nq = Q.nv, eq = Q.nedge;
+        const int64_t qrow = Q.row_begin + (tile - F.tile_begin) * 32 + lane;
+        const bool qlive = qrow < Q.row_end;
+        for (int p = 0; p < nq; ++p) qimg[lane * vs + p] = qlive ? __ldcs(a.gen_cols[p] + qrow) : -1;
+        if (ecols)
+            for (int j = 0; j < eq; ++j) qec[lane * es + j] = qlive ? __ldcs(a.gen_cols[a.gen_ecol + j] + qrow) : -1;
+
+        if (F.gen_kind == 2) {
+            // Backward tuple (target t, label el): the Q row itself, when its
+            // smallest unused closing edge label is el.
             bool ok = false;
-            int32_t bel = 0;
-            if (live) {
-                const int bv = P.back_v[t];
-                const int32_t x = img[bv];
-                const int32_t un = img[P.vn];
-                const uint32_t tlx = (uint32_t)P.vlab[bv];
+            int32_t bpos = 0;
+            if (qlive) {
+                const int t = F.gen_s;
+                const int bv = Q.back_v[t];
+                const int32_t x = qimg[lane * vs + bv];
+                const int32_t un = qimg[lane * vs + Q.vn];
+                const uint32_t tlx = (uint32_t)Q.vlab[bv];
                 const int32_t b = __ldg(a.offsets + un), e = __ldg(a.offsets + un + 1);
-                for (int32_t el = P.back_eq[t] ? P.back_el[t] : P.back_el[t] + 1; el < a.nel && !ok; ++el) {
+                for (int32_t el = Q.back_eq[t] ? Q.back_el[t] : Q.back_el[t] + 1; el < a.nel; ++el) {
                     const uint64_t want = pack_entry((uint32_t)el, tlx, (uint32_t)x);
                     int32_t pos;
                     if (a.eidx) {
@@ -1147,47 +1282,86 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 
                         pos = lower_bound_entry(a.adj, b, e, want);
                         if (pos >= e || __ldg(a.adj + pos) != want) pos = -1;
                     }
-                    if (pos >= 0) {
-                        // has_edge: the row already uses an edge (un, x, el).
-                        // Without self-loops images are distinct, so that is
-                        // a code edge joining v_n and the target.
-                        bool used = false;
-                        if (!a.loops && el < 32) {
-                            used = (P.back_used[t] >> el) & 1u;
-                        } else {
-                            for (int j = 0; j < P.nedge; ++j) {
-                                if (P.e_el[j] != el) continue;
-                                const int32_t f = img[P.e_from[j]], g2 = img[P.e_to[j]];
-                                if ((f == un && g2 == x) || (g2 == un && f == x)) used = true;
-                            }
-                        }
-                        if (!used) {
-                            ok = true;
-                            bel = el;
-                        }
+                    if (pos < 0) continue;
+                    bool used = false;
+                    for (int j = 0; j < eq; ++j) {
+                        if (Q.e_el[j] != el) continue;
+                        const int32_t f = qimg[lane * vs + Q.e_from[j]], g2 = qimg[lane * vs + Q.e_to[j]];
+                        if ((f == un && g2 == x) || (g2 == un && f == x)) used = true;
                     }
+                    if (used) continue;
+                    ok = el == F.gen_kc;
+                    bpos = pos;
+                    break;
                 }
             }
-            const int32_t bk = t * a.nel + bel;
-            const int32_t key = P.key_base + nsrc * K + bk;
-            const unsigned mask = __ballot_sync(kFull, ok);
-            if (ok) {
-                const unsigned peers = __match_any_sync(mask, key);
-                if (lane == __ffs(peers) - 1) atomicAdd(a.counts + key, (unsigned long long)__popc(peers));
+            for (int p = 0; p < nq; ++p) gimg[lane * vs + p] = qimg[lane * vs + p];
+            if (ecols) {
+                for (int j = 0; j < eq; ++j) gec[lane * es + j] = qec[lane * es + j];
+                gec[lane * es + eq] = bpos;
             }
-            if (mask) {
-                const int64_t out = P.sz_off + (int64_t)nsrc * K * (nv + 1);
-                for (int p = 0; p < nv; ++p) {
-                    const uint32_t got =
-                        ok ? or_fresh(a.MB + P.b_off + ((int64_t)p * P.nloc + (img[p] - P.vbase)) * P.bw + (bk >> 5),
-                                      1u << (bk & 31))
-                           : 0u;
-                    for (int w = 0; w < P.bw; ++w)
-                        add_fresh_bits((bk >> 5) == w ? got : 0u, a.sizes, out + p, nv, w, lane);
-                }
+            __syncwarp();
+            mask_row<MW>(a, F, gimg + lane * vs, EcolFromShared{gec + lane * es}, ok, lane);
+            __syncwarp();
+            continue;
+        }
+
+        // Forward tuple (source s, window key kc): the entries of the
+        // segment (s, kc) of each Q row's source image, minus the row's images.
+        int32_t st = 0, c = 0;
+        if (qlive) {
+            const int32_t u = qimg[lane * vs + Q.src_v[F.gen_s]];
+            const uint32_t kc = (uint32_t)F.gen_kc;
+            if (a.segstart) {
+                const int64_t K1 = (int64_t)a.nel * a.lwin + 1;
+                st = __ldg(a.segstart + (int64_t)u * K1 + kc);
+                c = __ldg(a.segstart + (int64_t)u * K1 + kc + 1) - st;
+            } else {
+                const int32_t b = __ldg(a.offsets + u), e = __ldg(a.offsets + u + 1);
+                const uint32_t el = kc / (uint32_t)a.lwin;
+                const uint32_t tl = (uint32_t)Q.lbase + kc % (uint32_t)a.lwin;
+                st = lower_bound_entry(a.adj, b, e, pack_entry(el, tl, 0));
+                c = lower_bound_entry(a.adj, st, e, pack_entry(el, tl + 1, 0)) - st;
             }
         }
+        wst[lane] = st;
+        wcnt[lane] = c;
+        int32_t incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t t = __shfl_up_sync(kFull, incl, d);
+            if (lane >= d) incl += t;
+        }
+        wpre[lane] = incl - c;
+        const int32_t total = __shfl_sync(kFull, incl, 31);
         __syncwarp();
+        for (int32_t base = 0; base < total; base += 32) {
+            const int32_t item = base + lane;
+            bool ok = item < total;
+            if (ok) {
+                int l2 = 0, h2 = 31;
+                while (l2 < h2) {
+                    const int mid = (l2 + h2 + 1) >> 1;
+                    if (wpre[mid] <= item) l2 = mid; else h2 = mid - 1;
+                }
+                const int owner = l2;
+                const int32_t ei = wst[owner] + (item - wpre[owner]);
+                const int32_t to = (int32_t)entry_to(__ldg(a.adj + ei));
+                for (int p = 0; p < nq; ++p) {
+                    const int32_t x = qimg[owner * vs + p];
+                    ok &= x != to;
+                    gimg[lane * vs + p] = x;
+                }
+                gimg[lane * vs + nq] = to;
+                if (ecols) {
+                    for (int j = 0; j < eq; ++j) gec[lane * es + j] = qec[owner * es + j];
+                    gec[lane * es + eq] = ei;
+                }
+            }
+            __syncwarp();
+            mask_row<MW>(a, F, gimg + lane * vs, EcolFromShared{gec + lane * es}, ok, lane);
+            __syncwarp();
+        }
     }
 }
 
@@ -1516,6 +1690,13 @@ MaskDev mask_dev(const MaskArgs& x)
     a.tile_counter = x.tile_counter;
     a.scanned = x.scanned;
     a.status = x.status;
+    a.gen_parents = x.gen_parents;
+    a.gen_cols = x.gen_cols;
+    a.gen_ecol = x.gen_ecol;
+    // gen_nv >= every generated row's vertices and pattern edges, so image
+    // p < nv and entry column j < nedge stay inside their strides.
+    a.gen_vs = (x.gen_nv + 1) | 1;
+    a.gen_es = (x.gen_nv + 1) | 1;
     return a;
 }
 
@@ -1538,6 +1719,29 @@ cudaError_t launch_mask_rows(const MaskArgs& x, cudaStream_t st)
         k_mask_rows<kNarrowMaskWords><<<grid, kMaskWarps * 32, 0, st>>>(mask_dev(x));
     else
         k_mask_rows<kMaxMaskWords><<<grid, kMaskWarps * 32, 0, st>>>(mask_dev(x));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mask_gen(const MaskArgs& x, cudaStream_t st)
+{
+    if (x.ntiles == 0) return cudaSuccess;
+    const MaskDev a = mask_dev(x);
+    const size_t smem = (size_t)kMaskWarps * gen_warp_ints(a.gen_vs, a.gen_es) * sizeof(int32_t);
+    const int64_t need = (x.ntiles + kMaskWarps - 1) / kMaskWarps;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    const int grid = (int)(need < cap ? need : cap);
+    cudaError_t e;
+    if (x.g->segw <= kNarrowMaskWords) {
+        if ((e = cudaFuncSetAttribute(k_mask_gen<kNarrowMaskWords>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem)) != cudaSuccess)
+            return e;
+        k_mask_gen<kNarrowMaskWords><<<grid, kMaskWarps * 32, smem, st>>>(a);
+    } else {
+        if ((e = cudaFuncSetAttribute(k_mask_gen<kMaxMaskWords>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem)) != cudaSuccess)
+            return e;
+        k_mask_gen<kMaxMaskWords><<<grid, kMaskWarps * 32, smem, st>>>(a);
+    }
     return cudaGetLastError();
 }
 

@@ -210,6 +210,20 @@ struct ActiveSet {
     }
 };
 
+// Two-level last step: the parents of the last level are not materialised but
+// generated from their own parents' rows by k_mask_gen.  Per parent of the
+// last level: its parent's index in `up` (metas of the level above, rows in
+// that level's table), the child tuple it is (kind 1 forward from source s with
+// window key kc, kind 2 backward to target s with edge label kc) and its
+// embedding count.
+struct GenSource {
+    std::vector<ParentMeta> up;
+    std::vector<int32_t> up_of;
+    std::vector<int16_t> kind, s;
+    std::vector<int32_t> kc;
+    std::vector<uint64_t> rows;
+};
+
 struct Run {
     gspan_ctx* ctx;
     const DevGraph& g;
@@ -480,6 +494,28 @@ struct Run {
         int support;
     };
 
+    // Whether the next-to-last level (children `freq` of the parents in
+    // `table`) is generated inside the last level's row pass rather than
+    // stored: opts.fused_last 2 always, 1 never, 0 when its table would take
+    // more than half the free device memory.  Only the mask path can take
+    // generated rows, so every child must fit its masks.
+    bool generate_last(const std::vector<Freq>& freq, const Table& table) const
+    {
+        const int mode = ctx->opts.fused_last;
+        if (mode == 1 || g.segw == 0 || ctx->opts.path == 1) return false;
+        double bytes = 0;
+        for (const Freq& f : freq) {
+            const int nback = (int)rightmost_path(f.code).size() - 1;
+            if ((int64_t)nback * g.nel > 32 * kMaxMaskWords) return false;
+            const int ncols = f.nvc + (table.ecol >= 0 ? (int)f.code.size() : 0);
+            bytes += 4.0 * ncols * (double)f.count;
+        }
+        if (mode == 2) return true;
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        return bytes > 0.5 * (double)free_b;
+    }
+
     // Materialisation readback waiting for a sync (see the end of level()).
     bool pending_scan = false;
     void settle()
@@ -506,7 +542,8 @@ struct Run {
         }
     }
 
-    gspan_status level(int size, std::vector<Parent>& parents, Table& table, std::vector<Parent>& next, Table& out)
+    gspan_status level(int size, std::vector<Parent>& parents, Table& table, std::vector<Parent>& next, Table& out,
+                       const GenSource* gen = nullptr)
     {
         const int32_t K = g.nel * g.lwin;
         const int np = (int)parents.size();
@@ -575,6 +612,14 @@ struct Run {
                         P.back_used[t] |= 1u << e.el;
             P.row_begin = parents[i].row_begin;
             P.row_end = parents[i].row_end;
+            if (gen) {
+                P.row_begin = 0;
+                P.row_end = (int64_t)gen->rows[i];
+                P.gen_p2 = gen->up_of[i];
+                P.gen_kind = gen->kind[i];
+                P.gen_s = gen->s[i];
+                P.gen_kc = gen->kc[i];
+            }
             P.key_base = (int32_t)nkeys;
             key_span[i] = (int64_t)P.nsrc * K + (int64_t)P.nback * g.nel;
             nkeys += key_span[i];
@@ -602,6 +647,11 @@ struct Run {
                 const double clear_words = (double)P.nsrc * (nv + 1) * P.nloc * g.segw + (double)nv * P.nloc * P.bw;
                 const double bias = ctx->opts.mask_bias > 0 ? ctx->opts.mask_bias : 1.0;
                 use_mask[i] = mode == 2 || (double)rows * P.nsrc * g.edge_biased_degree > 0.125 * bias * clear_words;
+            }
+            if (gen && !use_mask[i]) {
+                if (!(mask_possible && P.bw <= kMaxMaskWords))
+                    return fail(ctx, GSPAN_ERR_LIMIT, "generated last level needs the mask path");
+                use_mask[i] = 1;
             }
         }
 
@@ -647,7 +697,12 @@ struct Run {
                 groups.emplace_back();
             MGroup& G = groups.back();
             P.tile_begin = G.tiles;
-            G.tiles += (rows + 31) / 32;
+            if (gen) {
+                const ParentMeta& Q = gen->up[(size_t)P.gen_p2];
+                G.tiles += (Q.row_end - Q.row_begin + 31) / 32;
+            } else {
+                G.tiles += (rows + 31) / 32;
+            }
             P.r_off = G.r;
             G.r += rw;
             P.h_off = G.h;
@@ -675,12 +730,13 @@ struct Run {
         st.candidate_parents += cg.size();
 
         unsigned long long* d_counts = nullptr;
-        ParentMeta *d_mg = nullptr, *d_cg = nullptr, *d_all = nullptr;
+        ParentMeta *d_mg = nullptr, *d_cg = nullptr, *d_all = nullptr, *d_up = nullptr;
         uint32_t *d_R = nullptr, *d_H = nullptr, *d_M = nullptr, *d_MB = nullptr, *d_sizes = nullptr;
         uint32_t* d_tcount = nullptr;
         int32_t *d_touched = nullptr, *d_psp = nullptr;
         unsigned long long* d_tprefix = nullptr;
         auto release = [&]() {
+            dfree(d_up, s);
             dfree(d_counts, s);
             dfree(d_mg, s);
             dfree(d_cg, s);
@@ -705,6 +761,14 @@ struct Run {
         GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), s), "clear counters");
 
         cudaEvent_t e0, e1;
+        int32_t gen_nv = 0;
+        if (gen) {
+            GS_CK(dalloc(&d_up, gen->up.size(), s), "alloc generating parents");
+            GS_CK(copy(d_up, gen->up.data(), gen->up.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s),
+                  "copy generating parents");
+            for (const ParentMeta& P : meta) gen_nv = std::max<int32_t>(gen_nv, std::max<int32_t>(P.nv, P.nedge));
+            for (uint64_t r : gen->rows) st.fused_rows += r;
+        }
         if (!groups.empty()) {
             int64_t mr = 0, mh = 0, mm = 0, mb = 0, mt = 0, mps = 0, mmeta = 0;
             for (const MGroup& G : groups) {
@@ -760,7 +824,17 @@ struct Run {
                 ma.scanned = ctx->d_counters + 3;
                 ma.status = ctx->d_status;
                 tic(&e0, &e1);
-                GS_CK(launch_mask_rows(ma, s), "mask row pass launch");
+                if (gen) {
+                    ma.in_col_ptrs = nullptr;
+                    ma.ecol = table.ecol >= 0 ? 0 : -1;   // generated rows carry entry columns too
+                    ma.gen_parents = d_up;
+                    ma.gen_cols = table.d_cols;
+                    ma.gen_ecol = table.ecol;
+                    ma.gen_nv = gen_nv;
+                    GS_CK(launch_mask_gen(ma, s), "generated row pass launch");
+                } else {
+                    GS_CK(launch_mask_rows(ma, s), "mask row pass launch");
+                }
                 toc(e0, e1, &st.rows_ms);
                 tic(&e0, &e1);
                 GS_CK(launch_mask_sweep(ma, s), "mask sweep launch");
@@ -934,6 +1008,36 @@ struct Run {
             st.frontier_rows += f.count;
         }
         if (size + 1 >= k || freq.empty()) return GSPAN_OK;
+
+        // Next-to-last level: its rows may be generated from this level's
+        // rows inside the last level's row pass instead of being stored.
+        if (size + 2 == k && generate_last(freq, table)) {
+            GenSource gsrc;
+            gsrc.up = meta;
+            std::vector<Parent> last;
+            for (const Freq& f : freq) {
+                const int i = (int)(std::upper_bound(meta.begin(), meta.end(), f.key,
+                                                     [](int32_t k2, const ParentMeta& m2) { return k2 < m2.key_base; }) -
+                                    meta.begin()) - 1;
+                const int64_t lk = f.key - meta[i].key_base;
+                const int64_t nfwd = (int64_t)meta[i].nsrc * K;
+                gsrc.up_of.push_back(i);
+                if (lk < nfwd) {
+                    gsrc.kind.push_back(1);
+                    gsrc.s.push_back((int16_t)(lk / K));
+                    gsrc.kc.push_back((int32_t)(lk % K));
+                } else {
+                    gsrc.kind.push_back(2);
+                    gsrc.s.push_back((int16_t)((lk - nfwd) / g.nel));
+                    gsrc.kc.push_back((int32_t)((lk - nfwd) % g.nel));
+                }
+                gsrc.rows.push_back(f.count);
+                last.push_back(Parent{f.code, 0, (int64_t)f.count});
+            }
+            std::vector<Parent> none;
+            Table unused;
+            return level(size + 1, last, table, none, unused, &gsrc);
+        }
 
         // Materialise the frequent children, grouped by tuple (offsets from the
         // counts: a one-digit counting sort of the candidates by DFS tuple).

@@ -10,6 +10,9 @@
 //   --domains auto|bitmap|hash
 //   --hash-threshold X     auto domains: hashset when 64 * size < |V| * X
 //   --device N
+//   --fused-last auto|off|always
+//                          next-to-last level generated inside the last
+//                          level's row pass instead of stored
 //   --prune                drop vertices of labels with fewer than min_support
 //                          vertices before mining (the reference's prune_graph,
 //                          left commented out at fsm.cu:28-29); same output
@@ -73,6 +76,12 @@ Options parse(int argc, char* argv[])
             opt.o.hash_threshold = std::atof(value().c_str());
         } else if (a == "--device") {
             opt.o.device = std::atoi(value().c_str());
+        } else if (a == "--fused-last") {
+            const std::string v = value();
+            if (v == "auto") opt.o.fused_last = 0;
+            else if (v == "off") opt.o.fused_last = 1;
+            else if (v == "always") opt.o.fused_last = 2;
+            else throw std::runtime_error("--fused-last: auto, off or always");
         } else if (a == "--prune") {
             opt.o.prune = 1;
         } else {
@@ -123,7 +132,7 @@ int main(int argc, char* argv[])
 {
     if (argc < 4) {
         std::printf("usage: %s input_graph min_support k [--text] [--path auto|candidate|mask] "
-                    "[--domains auto|bitmap|hash] [--hash-threshold X] [--device N] [--prune] [--stats]\n",
+                    "[--domains auto|bitmap|hash] [--hash-threshold X] [--device N] [--fused-last auto|off|always] [--prune] [--stats]\n",
                     argv[0]);
         return 0;
     }

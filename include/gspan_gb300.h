@@ -70,6 +70,10 @@ typedef struct gspan_opts {
                                     prune_graph, graph.cc:216-266, done on the device).  Patterns and
                                     supports are unchanged; `extended` then counts the pruned graph's
                                     children.  Ignored for batches.  Default 0 */
+    int32_t fused_last;          /* the next-to-last level's embeddings: 0 auto (generated on the fly inside the
+                                    last level's row pass when storing them would take more than half the free
+                                    device memory, else stored), 1 always stored, 2 always generated (needs the
+                                    mask path; both give identical results) */
 } gspan_opts;
 
 /* Run statistics.  Counts are exact and identical to those of the reference's
@@ -109,6 +113,8 @@ typedef struct gspan_stats {
     double canonical_ms;         /* host time in tests not already done while the GPU counted */
     uint64_t pruned_vertices;    /* opts.prune: vertices dropped before mining (0 otherwise) */
     uint64_t pruned_entries;     /* opts.prune: directed entries dropped with them */
+    uint64_t fused_rows;         /* next-to-last-level embeddings generated inside the last level's row pass
+                                    instead of being stored */
 } gspan_stats;
 
 typedef struct gspan_ctx gspan_ctx;

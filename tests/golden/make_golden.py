@@ -21,6 +21,7 @@ large_manifest.json with the job's extended-embedding count.
 
     python tests/golden/make_golden.py --large
 """
+import gzip
 import hashlib
 import json
 import os
@@ -55,6 +56,11 @@ CASES = [
 # (name, generator call, min_support, k)
 LARGE_CASES = [
     ("chung_lu_100k", "datagen.chung_lu_100k(1)", 10000, 3),
+    # The 3.7M-vertex configuration (exponent 2.3, degree cap sqrt(2m), 37
+    # labels Zipf(0.8), seed 3) scaled to 20,000 vertices with the same mean
+    # degree, min support scaled likewise (20,000 x 20,000 / 3.7M), 4 edges.
+    ("chung_lu_3_7m_scaled_20k", "datagen.chung_lu(20000, 89189, 2.3, 37, 0.8, 3, max_deg=(2 * 89189) ** 0.5)",
+     108, 4),
 ]
 
 
@@ -72,9 +78,16 @@ def make_large() -> None:
             out = r.stdout.splitlines()
             assert out and out[-1].startswith("load:"), out[-1:]
             st = json.loads(r.stderr.strip().splitlines()[-1])
+            body = "".join(line + "\n" for line in out[:-1]).encode()
             fname = f"{name}_s{sup}_k{k}.txt"
-            with open(os.path.join(HERE, fname), "w") as f:
-                f.write("".join(line + "\n" for line in out[:-1]))
+            if len(body) > 64 << 10:   # long outputs are stored gzipped (fixed mtime: reproducible bytes)
+                fname += ".gz"
+                with open(os.path.join(HERE, fname), "wb") as raw:
+                    with gzip.GzipFile(fileobj=raw, mode="wb", mtime=0) as f:
+                        f.write(body)
+            else:
+                with open(os.path.join(HERE, fname), "wb") as f:
+                    f.write(body)
             manifest.append({"name": name, "graph": expr, "sha256": hashlib.sha256(g.to_bytes()).hexdigest(),
                              "min_support": sup, "k": k, "expected": fname, "patterns": len(out) - 1,
                              "seeds": st["seeds"], "extended": st["extended"],

@@ -51,7 +51,12 @@ def golden_graph(case):
 
 
 def golden_lines(case):
-    with open(os.path.join(GOLDEN, case["expected"])) as f:
+    path = os.path.join(GOLDEN, case["expected"])
+    if path.endswith(".gz"):
+        import gzip
+        with gzip.open(path, "rt") as f:
+            return f.read().splitlines()
+    with open(path) as f:
         return f.read().splitlines()
 
 
