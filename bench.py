@@ -433,7 +433,7 @@ def batch_arm(args) -> None:
     import torch
     from gspan_gb300 import Miner, datagen
     count = 256 if args.workload == "batch_256" else 16
-    k = 3
+    k = args.batch_k
     t0 = time.time()
     graphs, sups = datagen.batch_instances(2, count)
     gen_s = time.time() - t0
@@ -441,7 +441,7 @@ def batch_arm(args) -> None:
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     from gspan_gb300 import decode_results
-    with Miner(profile=True) as m:
+    with Miner(profile=True, fused_last=args.fused_last) as m:
         bg = m.upload_batch(graphs)
         singles = [m.upload(g) for g in graphs]
         for _ in range(args.warmup):
@@ -479,11 +479,12 @@ def batch_arm(args) -> None:
         "config": {"workload": args.workload, "instances": count, "k": k,
                    "description": "Chung-Lu instances, n log-uniform in [1k, 200k], average degree U[4, 24], "
                                   "8-32 vertex labels Zipf(1.0), exponent 2.1, degree cap sqrt(2m), "
-                                  "min support 2% of n, seed 2; patterns up to 3 edges",
-                   "engine": "batched"},
+                                  f"min support 2% of n, seed 2; patterns up to {k} edges",
+                   "engine": "batched", "fused_last": ["auto", "off", "always"][args.fused_last]},
         "plain": {"value": pval, "ms_per_step": statistics.median(plain_ms)},
         "batched_over_plain": bval / pval,
-        "extended_per_step": ext, "patterns": st["patterns"], "generate_s": gen_s, "clocks": clocks,
+        "extended_per_step": ext, "patterns": st["patterns"], "fused_rows_per_step": st["fused_rows"],
+        "generate_s": gen_s, "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
 
@@ -632,6 +633,7 @@ def main() -> None:
     ap.add_argument("--fused-last", type=int, default=0, choices=[0, 1, 2],
                     help="next-to-last level: 0 auto, 1 stored, 2 generated inside the last row pass")
     ap.add_argument("--prune", action="store_true", help="drop vertices of infrequent labels before mining")
+    ap.add_argument("--batch-k", type=int, default=4, help="batch_256 / batch_16: pattern size in edges")
     ap.add_argument("--slots", type=int, default=4, help="serving: concurrent contexts")
     ap.add_argument("--serving-jobs", type=int, default=100, help="serving: jobs per stream (one step)")
     ap.add_argument("--rate", type=float, default=50.0, help="serving: mean arrivals per second (0: all at once)")

@@ -26,7 +26,8 @@ namespace {
 __global__ void k_rank_hist(int32_t n, const int32_t* __restrict__ vrank, unsigned long long* __restrict__ hist)
 {
     const int lane = threadIdx.x & 31;
-    for (int64_t base = (blockIdx.x * (int64_t)blockDim.x) & ~31ll; base < n;
+    // Warp per 32 consecutive vertices (the stride is a multiple of 32).
+    for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; base < n;
          base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t v = base + lane;
         const bool live = v < n;
