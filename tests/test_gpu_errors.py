@@ -34,9 +34,10 @@ def test_out_of_memory_leaves_context_usable():
         torch.cuda.synchronize()
         used0 = _pool_used_bytes()
         for _ in range(2):
-            # Four-edge patterns at support 1,000 need terabytes of embeddings.
+            # Five-edge patterns at support 1,000: the stored three-edge table
+            # alone would take terabytes (only the four-edge level is generated).
             with pytest.raises(GspanError) as e:
-                m.mine(dbig, 4, 1000)
+                m.mine(dbig, 5, 1000)
             assert e.value.status == GSPAN_ERR_NOMEM
             torch.cuda.synchronize()
             if used0 is not None:

@@ -74,7 +74,7 @@ def test_out_of_memory_job_among_others():
     with Server(slots=3) as srv:
         gs_, gb = srv.add_graph(small), srv.add_graph(big)
         hs = [srv.submit(gs_, 3, 20) for _ in range(3)]
-        hb = srv.submit(gb, 4, 1000)         # four-edge patterns at support 1,000: terabytes of embeddings
+        hb = srv.submit(gb, 5, 1000)         # five-edge patterns at support 1,000: terabytes of embeddings
         hs += [srv.submit(gs_, 3, 20) for _ in range(3)]
         for h in hs:
             got, info = srv.wait(h)

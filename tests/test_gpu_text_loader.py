@@ -22,7 +22,7 @@ ODD = (
     "e 7 10 1\n"               # 7 is never declared: label 0
     "e 7 7 0\n"                # self-loop
     "e 10 -5 0\n"              # parallel edge
-    "x junk tokens 12\n"       # skipped
+    "x junk words 12\n"        # skipped (no token starts with t, v or e)
     "t # 1\n"
     "v 1000000 2\n"
     "e 1000000 7 0\n"
