@@ -78,3 +78,20 @@ def test_edge_outside_its_instance_is_rejected():
             m.mine(bg, 2, 1)     # a batch is mined with mine_batch
         with pytest.raises(ValueError):
             m.mine_batch(bg, 2, [1])
+
+
+def test_generated_last_level_in_a_batch():
+    """A batch at 4 edges with the 3-edge level generated inside the 4-edge
+    row pass (fused_last = 2): every instance equals the oracle, and the
+    instances' windows keep generated rows apart."""
+    from gspan_gb300 import Miner
+    graphs, sups = _instances()
+    with Miner(fused_last=2) as m:
+        got, st = m.mine_batch(m.upload_batch(graphs), 4, sups)
+    assert st["fused_rows"] > 0
+    ext = 0
+    for i, (g, s) in enumerate(zip(graphs, sups)):
+        lines, ref = run_port(g, s, 4, threads=4, with_stats=True, stream_last=True)
+        assert lines_of(got[i]) == lines, i
+        ext += ref["extended"]
+    assert st["extended"] == ext
