@@ -246,7 +246,7 @@ cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d
                                    uint32_t* d_status, cudaStream_t st);
 cudaError_t launch_seed_count(const DevGraph& g, unsigned long long* counts, cudaStream_t st);
 // col2 (may be null) receives each seed's entry index.
-cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* pool, int32_t* col0,
+cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, int32_t nact, uint32_t* pool, int32_t* col0,
                                 int32_t* col1, int32_t* col2, uint32_t* status, cudaStream_t st);
 cudaError_t launch_expand(const ExpandArgs& a, Pass pass, cudaStream_t st);
 cudaError_t launch_domain_sizes(const DomDesc* dom, int32_t nact, const uint32_t* pool,

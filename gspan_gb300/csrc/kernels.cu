@@ -152,11 +152,28 @@ __global__ void k_label_minmax(int32_t n, const int32_t* __restrict__ vlabels, i
         emin = min(emin, __shfl_xor_sync(kFull, emin, o));
         emax = max(emax, __shfl_xor_sync(kFull, emax, o));
     }
+    // Block-wide first, so the four global words see one atomic per block
+    // instead of one per warp.
+    __shared__ int32_t part[4][32];
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        atomicMin(out + 0, vmin);
-        atomicMax(out + 1, vmax);
-        atomicMin(out + 2, emin);
-        atomicMax(out + 3, emax);
+        part[0][w] = vmin;
+        part[1][w] = vmax;
+        part[2][w] = emin;
+        part[3][w] = emax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < nw; ++q) {
+            vmin = min(vmin, part[0][q]);
+            vmax = max(vmax, part[1][q]);
+            emin = min(emin, part[2][q]);
+            emax = max(emax, part[3][q]);
+        }
+        if (vmin != INT32_MAX) atomicMin(out + 0, vmin);
+        if (vmax != INT32_MIN) atomicMax(out + 1, vmax);
+        if (emin != INT32_MAX) atomicMin(out + 2, emin);
+        if (emax != INT32_MIN) atomicMax(out + 3, emax);
     }
 }
 
@@ -164,11 +181,29 @@ __global__ void k_label_presence(int32_t n, const int32_t* __restrict__ vlabels,
                                  uint8_t* __restrict__ vflag, int32_t m, const gspan_edge* __restrict__ edges,
                                  int32_t elo, uint8_t* __restrict__ eflag)
 {
+    // Few distinct labels over many elements: one writer per distinct label
+    // per warp, and only where the flag is not yet set (a read, not a store,
+    // for the common case).  The loops are warp-uniform (stride and bounds
+    // rounded to whole warps).
+    const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
-        vflag[(int64_t)vlabels[i] - vlo] = 1;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride)
-        eflag[(int64_t)edges[i].label - elo] = 1;
+    const int64_t first = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll;
+    for (int64_t base = first; base < n; base += stride) {
+        const int64_t i = base + lane;
+        const bool live = i < n;
+        const int32_t x = live ? vlabels[i] : 0;
+        const unsigned lm = __ballot_sync(kFull, live);
+        if (live && lane == __ffs(__match_any_sync(lm, x)) - 1 && !vflag[(int64_t)x - vlo])
+            vflag[(int64_t)x - vlo] = 1;
+    }
+    for (int64_t base = first; base < m; base += stride) {
+        const int64_t i = base + lane;
+        const bool live = i < m;
+        const int32_t x = live ? edges[i].label : 0;
+        const unsigned lm = __ballot_sync(kFull, live);
+        if (live && lane == __ffs(__match_any_sync(lm, x)) - 1 && !eflag[(int64_t)x - elo])
+            eflag[(int64_t)x - elo] = 1;
+    }
 }
 
 __device__ __forceinline__ int32_t last_at_most(const int64_t* base, int32_t n, int64_t x)
@@ -358,10 +393,23 @@ __device__ __forceinline__ bool seed_key(const int32_t* __restrict__ src, const 
     return fl <= tl && (uint32_t)local < (uint32_t)lwin;
 }
 
+// Seed tuples whose block-level counters fit shared memory (8 bytes each).
+constexpr int kSeedSmemKeys = 4096;
+
+// Embedding count per seed tuple.  With `smem_keys` > 0 (the key space fits
+// shared memory), each block counts into its own histogram first and adds
+// its non-zero bins once, so the few hot tuples (frequent label pairs) take
+// one global atomic per block instead of one per warp.
 __global__ void k_seed_count(int32_t m, const int32_t* __restrict__ src, const uint64_t* __restrict__ adj,
                              const int32_t* __restrict__ vrank, const int32_t* __restrict__ win_base, int32_t lwin,
-                             int32_t nel, unsigned long long* __restrict__ counts)
+                             int32_t nel, unsigned long long* __restrict__ counts, int32_t smem_keys)
 {
+    extern __shared__ unsigned long long seed_hist[];
+    if (smem_keys > 0) {
+        for (int32_t q = threadIdx.x; q < smem_keys; q += blockDim.x) seed_hist[q] = 0;
+        __syncthreads();
+    }
+    unsigned long long* const tgt = smem_keys > 0 ? seed_hist : counts;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -378,21 +426,59 @@ __global__ void k_seed_count(int32_t m, const int32_t* __restrict__ src, const u
         if ((heads >> lane) & 1u) {
             const unsigned stop = (heads | ~okm) & ~((2u << lane) - 1u);
             const int end = stop ? __ffs(stop) - 1 : 32;
-            atomicAdd(counts + key, (unsigned long long)(end - lane));
+            atomicAdd(tgt + key, (unsigned long long)(end - lane));
         }
+    }
+    if (smem_keys > 0) {
+        __syncthreads();
+        for (int32_t q = threadIdx.x; q < smem_keys; q += blockDim.x)
+            if (seed_hist[q]) atomicAdd(counts + q, seed_hist[q]);
     }
 }
 
+// Seed domains and (when materialising) the level-1 table.  With `smem_act` >
+// 0 (the active tuples fit shared memory), a block first counts its rows per
+// active tuple, reserves one range per tuple in the global cursor, and then
+// hands out slots from a shared cursor, so the hot tuples' global cursors
+// take one atomic per block.  Rows of a tuple may land in any order.
 __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const uint64_t* __restrict__ adj,
                                const int32_t* __restrict__ vrank, const int32_t* __restrict__ win_base,
                                int32_t lwin, int32_t nel, LevelKeys keys,
                                uint32_t* __restrict__ pool, int32_t* __restrict__ col0, int32_t* __restrict__ col1,
-                               int32_t* __restrict__ col2,
-                               uint32_t* status)
+                               int32_t* __restrict__ col2, uint32_t* status, int32_t smem_act)
 {
+    extern __shared__ unsigned long long seed_cur[];   // [smem_act] block counts, then [smem_act] cursors
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool local = smem_act > 0 && col0 != nullptr;
+    if (local) {
+        for (int32_t q = threadIdx.x; q < 2 * smem_act; q += blockDim.x) seed_cur[q] = 0;
+        __syncthreads();
+        // This block's rows per active tuple (the same entries, in the same
+        // order, as the pass below).
+        for (int64_t base = warp * 32; base < m; base += nwarps * 32) {
+            const int64_t i = base + lane;
+            int32_t key = 0;
+            uint32_t u = 0, w = 0;
+            bool ok = i < m && seed_key(src, adj, vrank, win_base, lwin, nel, i, &key, &u, &w);
+            const int32_t a = ok ? keys.act[key] : -1;
+            const bool mat = a >= 0 && keys.mat_off[a] >= 0;
+            const unsigned mm = __ballot_sync(kFull, mat);
+            const int32_t prev = __shfl_up_sync(kFull, a, 1);
+            const unsigned heads = __ballot_sync(kFull, mat && (lane == 0 || !((mm >> (lane - 1)) & 1u) || prev != a));
+            if ((heads >> lane) & 1u) {
+                const unsigned stop = (heads | ~mm) & ~((2u << lane) - 1u);
+                const int end = stop ? __ffs(stop) - 1 : 32;
+                atomicAdd(seed_cur + a, (unsigned long long)(end - lane));
+            }
+        }
+        __syncthreads();
+        for (int32_t q = threadIdx.x; q < smem_act; q += blockDim.x)
+            if (seed_cur[q]) seed_cur[smem_act + q] = atomicAdd(keys.cursor + q, seed_cur[q]);
+        __syncthreads();
+    }
+    unsigned long long* const cursor = local ? seed_cur + smem_act : keys.cursor;
     for (int64_t base = warp * 32; base < m; base += nwarps * 32) {
         const int64_t i = base + lane;
         int32_t key = 0;
@@ -419,7 +505,7 @@ __global__ void k_seed_support(int32_t m, const int32_t* __restrict__ src, const
             const unsigned stop = (heads | ~mm) & ~((2u << h) - 1u);
             const int end = stop ? __ffs(stop) - 1 : 32;
             unsigned long long at = 0;
-            if (lane == h) at = atomicAdd(keys.cursor + a, (unsigned long long)(end - h));
+            if (lane == h) at = atomicAdd(cursor + a, (unsigned long long)(end - h));
             at = __shfl_sync(mm, at, h);
             const unsigned long long slot = at + (unsigned long long)(lane - h);
             if (slot < keys.counts[key]) {
@@ -463,7 +549,8 @@ struct ExpandDev {
 // [32][ss] (per row and range: first adjacency entry, entries), pre [32]
 // (exclusive prefix of the rows' entry counts).  vs, ss are odd (no bank
 // conflicts between lanes).
-__host__ __device__ inline int expand_warp_ints(int vs, int ss) { return 32 * (vs + 2 * ss + 1); }
+// Materialize also keeps a per-slot 64-bit cursor [ss] (2 * ss ints) after them.
+__host__ __device__ inline int expand_warp_ints(int vs, int ss) { return 32 * (vs + 2 * ss + 1) + 2 * ss; }
 
 template <Pass kPass>
 __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
@@ -473,6 +560,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
     int32_t* const Wstart = Wimg + 32 * a.vs;
     int32_t* const Wcnt = Wstart + 32 * a.ss;
     int32_t* const Wpre = Wcnt + 32 * a.ss;
+    unsigned long long* const Wcur = reinterpret_cast<unsigned long long*>(Wpre + 32);
     const int lane = threadIdx.x & 31;
     const int32_t LeLv = a.nel * a.lwin;
 
@@ -621,6 +709,89 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                     }
                 }
             }
+        }
+
+        if (kPass == Pass::Materialize && segs) {
+            // Few frequent tuples, one per slot: count the tile's rows per
+            // slot, reserve each slot's range with one global atomic, then
+            // write from a per-warp cursor (the hot tuples' global cursors
+            // see one atomic per tile instead of one per 32 candidates).
+            // The candidate of item: its owner row, slot and entry, and
+            // whether it is a child (its `to` not an image of the row).
+            auto candidate = [&](int32_t item, int* owner, int* slot, int32_t* eidx, uint32_t* to) {
+                int l2 = 0, h2 = 31;
+                while (l2 < h2) {
+                    const int mid = (l2 + h2 + 1) >> 1;
+                    if (Wpre[mid] <= item) l2 = mid; else h2 = mid - 1;
+                }
+                *owner = l2;
+                int32_t j = item - Wpre[l2];
+                int q = 0;
+                while (j >= Wcnt[l2 * a.ss + q]) {
+                    j -= Wcnt[l2 * a.ss + q];
+                    ++q;
+                }
+                *slot = q;
+                *eidx = Wstart[l2 * a.ss + q] + j;
+                *to = entry_to(__ldg(a.adj + *eidx));
+                bool fresh = true;
+                for (int p = 0; p < nv; ++p) fresh &= Wimg[l2 * a.vs + p] != (int32_t)*to;
+                return fresh;
+            };
+            if (lane < nslot) Wcur[lane] = 0;
+            __syncwarp();
+            for (int32_t base = 0; base < total; base += 32) {
+                int owner = 0, q = 0;
+                int32_t ei = 0;
+                uint32_t to = 0;
+                const bool ok = base + lane < total && candidate(base + lane, &owner, &q, &ei, &to);
+                const unsigned m = __ballot_sync(kFull, ok);
+                if (ok) {
+                    const unsigned peers = __match_any_sync(m, q);
+                    if (lane == __ffs(peers) - 1) atomicAdd(Wcur + q, (unsigned long long)__popc(peers));
+                }
+            }
+            __syncwarp();
+            if (lane < nslot) {
+                const int32_t key = key_base + P.mseg_s[lane] * LeLv + (int32_t)P.mseg_kc[lane];
+                const int32_t ai = a.keys.act[key];
+                const unsigned long long n = Wcur[lane];
+                Wcur[lane] = (n && ai >= 0) ? atomicAdd(a.keys.cursor + ai, n) : 0ull;
+            }
+            __syncwarp();
+            for (int32_t base = 0; base < total; base += 32) {
+                int owner = 0, q = 0;
+                int32_t ei = 0;
+                uint32_t to = 0;
+                const bool ok = base + lane < total && candidate(base + lane, &owner, &q, &ei, &to);
+                const int32_t key = key_base + P.mseg_s[q] * LeLv + (int32_t)P.mseg_kc[q];
+                const int32_t ai = ok ? a.keys.act[key] : -1;
+                const bool mat = ai >= 0;
+                const unsigned mm = __ballot_sync(kFull, mat);
+                if (mat) {
+                    const unsigned peers = __match_any_sync(mm, q);
+                    const int leader = __ffs(peers) - 1;
+                    unsigned long long at = 0;
+                    if (lane == leader) at = atomicAdd(Wcur + q, (unsigned long long)__popc(peers));
+                    at = __shfl_sync(mm, at, leader);
+                    const unsigned long long slot = at + __popc(peers & lanemask_lt());
+                    if (slot < a.keys.counts[key]) {
+                        const long long r = a.keys.mat_off[ai] + (long long)slot;
+                        for (int p = 0; p < nv; ++p) a.out_cols[p][r] = Wimg[owner * a.vs + p];
+                        a.out_cols[nv][r] = (int32_t)to;
+                        if (a.ecol_out >= 0) {
+                            const int64_t orow = P.row_begin + (tile - P.tile_begin) * kRows + owner;
+                            for (int jj = 0; jj < P.nedge; ++jj)
+                                a.out_cols[a.ecol_out + jj][r] = __ldg(a.in_cols[a.ecol_in + jj] + orow);
+                            a.out_cols[a.ecol_out + P.nedge][r] = ei;
+                        }
+                    } else {
+                        atomicOr(a.status, kErrCursor);
+                    }
+                }
+            }
+            __syncwarp();
+            continue;
         }
 
         // Forward candidates: the tile's adjacency ranges, 32 entries at a time.
@@ -912,9 +1083,44 @@ struct EcolFromShared {
 // source images), H and M for every source, and counts and MB masks for
 // backward tuples (at most one per row and rightmost-path target).  `img` holds
 // the lane's row images; lanes with !live take part in the warp-wide steps only.
+// Warp-uniform running sums of backward-tuple counts (one edge label: one
+// tuple per parent and target), added to the global counts when the key
+// changes and at the end of the kernel, instead of one atomic per row batch
+// on a handful of hot counters.
+struct BackAcc {
+    static constexpr int kTargets = 2;
+    // Per-warp slots in shared memory, touched by lane 0 only.
+    int32_t* key;                  // [kTargets], -1 when empty
+    unsigned long long* n;         // [kTargets]
+    __device__ __forceinline__ void init(int lane)
+    {
+        if (lane == 0)
+            for (int t = 0; t < kTargets; ++t) {
+                key[t] = -1;
+                n[t] = 0;
+            }
+    }
+    __device__ __forceinline__ void add(unsigned long long* counts, int t, int32_t k, unsigned long long c, int lane)
+    {
+        if (lane != 0) return;
+        if (key[t] != k) {
+            if (n[t]) atomicAdd(counts + key[t], n[t]);
+            key[t] = k;
+            n[t] = 0;
+        }
+        n[t] += c;
+    }
+    __device__ __forceinline__ void flush(unsigned long long* counts, int lane)
+    {
+        if (lane != 0) return;
+        for (int t = 0; t < kTargets; ++t)
+            if (n[t]) atomicAdd(counts + key[t], n[t]);
+    }
+};
+
 template <int MW, class Ecol>
 __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, const int32_t* img, const Ecol& ecol,
-                                         bool live, int lane)
+                                         bool live, int lane, BackAcc& acc)
 {
     const int32_t K = a.nel * a.lwin;
     const int mw = a.mw;
@@ -1177,7 +1383,11 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
         const int32_t bk = t * a.nel + bel;
         const int32_t key = P.key_base + nsrc * K + bk;
         const unsigned mask = __ballot_sync(kFull, ok);
-        if (ok) {
+        if (a.nel == 1 && t < BackAcc::kTargets) {
+            // One edge label: one backward tuple per target, the same in
+            // every lane; summed per warp and added once per parent.
+            if (mask) acc.add(a.counts, t, key, (unsigned long long)__popc(mask), lane);
+        } else if (ok) {
             const unsigned peers = __match_any_sync(mask, key);
             if (lane == __ffs(peers) - 1) atomicAdd(a.counts + key, (unsigned long long)__popc(peers));
         }
@@ -1203,6 +1413,10 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 
     int32_t (*img_all)[kMaxV + 1] = img_s[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     int32_t* img = img_all[lane];
+    __shared__ int32_t acc_key[kMaskWarps][BackAcc::kTargets];
+    __shared__ unsigned long long acc_n[kMaskWarps][BackAcc::kTargets];
+    BackAcc acc{acc_key[threadIdx.x >> 5], acc_n[threadIdx.x >> 5]};
+    acc.init(lane);
 
     for (;;) {
         long long tile = 0;
@@ -1214,9 +1428,10 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 
         const int64_t row = P.row_begin + (tile - P.tile_begin) * 32 + lane;
         const bool live = row < P.row_end;
         for (int p = 0; p < nv; ++p) img[p] = live ? __ldcs(a.in_cols[p] + row) : -1;
-        mask_row<MW>(a, P, img, EcolFromTable{a.in_cols, a.ecol, row}, live, lane);
+        mask_row<MW>(a, P, img, EcolFromTable{a.in_cols, a.ecol, row}, live, lane, acc);
         __syncwarp();
     }
+    acc.flush(a.counts, lane);
 }
 
 // Two-level last step: warp per tile of 32 rows of a parent's own parent Q
@@ -1246,6 +1461,10 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 4 : 
     int32_t* const wcnt = wst + 32;
     int32_t* const wpre = wcnt + 32;
     const bool ecols = a.gen_ecol >= 0;
+    __shared__ int32_t acc_key[kMaskWarps][BackAcc::kTargets];
+    __shared__ unsigned long long acc_n[kMaskWarps][BackAcc::kTargets];
+    BackAcc acc{acc_key[threadIdx.x >> 5], acc_n[threadIdx.x >> 5]};
+    acc.init(lane);
 
     for (;;) {
         long long tile = 0;
@@ -1301,7 +1520,7 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 4 : 
                 gec[lane * es + eq] = bpos;
             }
             __syncwarp();
-            mask_row<MW>(a, F, gimg + lane * vs, EcolFromShared{gec + lane * es}, ok, lane);
+            mask_row<MW>(a, F, gimg + lane * vs, EcolFromShared{gec + lane * es}, ok, lane, acc);
             __syncwarp();
             continue;
         }
@@ -1359,10 +1578,11 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 4 : 
                 }
             }
             __syncwarp();
-            mask_row<MW>(a, F, gimg + lane * vs, EcolFromShared{gec + lane * es}, ok, lane);
+            mask_row<MW>(a, F, gimg + lane * vs, EcolFromShared{gec + lane * es}, ok, lane, acc);
             __syncwarp();
         }
     }
+    acc.flush(a.counts, lane);
 }
 
 // Exclusive prefix of the touched-list lengths: the sweep's task numbering.
@@ -1484,6 +1704,14 @@ __global__ void k_domain_sizes(const DomDesc* __restrict__ dom, const uint32_t* 
     }
 }
 
+int sm_count()
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
 int grid_for(int64_t work, int threads)
 {
     int dev = 0, sms = 0;
@@ -1546,17 +1774,23 @@ cudaError_t launch_build_adjacency(const int32_t* d_offsets, const gspan_edge* d
 cudaError_t launch_seed_count(const DevGraph& g, unsigned long long* counts, cudaStream_t st)
 {
     if (g.m == 0) return cudaSuccess;
-    k_seed_count<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.win_base, g.lwin, g.nel, counts);
+    const int64_t nkeys = (int64_t)g.nvl * g.nel * g.lwin;
+    const int32_t smem_keys = nkeys <= kSeedSmemKeys ? (int32_t)nkeys : 0;
+    // Few blocks when each flushes a histogram: a couple per SM.
+    const int grid = smem_keys ? std::min(grid_for(g.m, 256), sm_count() * 2) : grid_for(g.m, 256);
+    k_seed_count<<<grid, 256, (size_t)smem_keys * 8, st>>>(g.m, g.src, g.adj, g.vrank, g.win_base, g.lwin, g.nel,
+                                                          counts, smem_keys);
     return cudaGetLastError();
 }
 
-cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, uint32_t* pool, int32_t* col0, int32_t* col1,
-                                int32_t* col2,
-                                uint32_t* status, cudaStream_t st)
+cudaError_t launch_seed_support(const DevGraph& g, LevelKeys keys, int32_t nact, uint32_t* pool, int32_t* col0,
+                                int32_t* col1, int32_t* col2, uint32_t* status, cudaStream_t st)
 {
     if (g.m == 0) return cudaSuccess;
-    k_seed_support<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.adj, g.vrank, g.win_base, g.lwin, g.nel, keys, pool,
-                                                       col0, col1, col2, status);
+    const int32_t smem_act = nact <= kSeedSmemKeys / 2 ? nact : 0;
+    const int grid = smem_act && col0 ? std::min(grid_for(g.m, 256), sm_count() * 2) : grid_for(g.m, 256);
+    k_seed_support<<<grid, 256, (size_t)smem_act * 16, st>>>(g.m, g.src, g.adj, g.vrank, g.win_base, g.lwin, g.nel,
+                                                            keys, pool, col0, col1, col2, status, smem_act);
     return cudaGetLastError();
 }
 
@@ -1700,13 +1934,6 @@ MaskDev mask_dev(const MaskArgs& x)
     return a;
 }
 
-int sm_count()
-{
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms;
-}
 }  // namespace
 
 cudaError_t launch_mask_rows(const MaskArgs& x, cudaStream_t st)

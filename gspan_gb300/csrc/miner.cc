@@ -417,7 +417,7 @@ struct Run {
         if (rc != GSPAN_OK) return rc;
         LevelKeys keys{d_counts, as.d_act, as.d_dom, as.d_mat, as.d_cursor};
         if (as.nact > 0) {
-            GS_CK(launch_seed_support(g, keys, as.pool, mat ? table.cols[0] : nullptr, mat ? table.cols[1] : nullptr,
+            GS_CK(launch_seed_support(g, keys, as.nact, as.pool, mat ? table.cols[0] : nullptr, mat ? table.cols[1] : nullptr,
                                       mat && table.ecol >= 0 ? table.cols[table.ecol] : nullptr, ctx->d_status, s),
                   "seed support launch");
             ++st.kernel_launches;
