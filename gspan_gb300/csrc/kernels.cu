@@ -1597,6 +1597,9 @@ __global__ void k_mask_prefix(int32_t nps, const uint32_t* __restrict__ tcount, 
     tprefix[nps] = run;
 }
 
+// Tuples per source whose forward counts a sweep warp sums in shared memory.
+constexpr int kSweepAccKeys = 64;
+
 // Sweep: warp per touched (parent, source, vertex u) over u's entries in the
 // source's range: child counts by tuple and the new vertex's domain masks.
 // R[u] and the H entries it reads are reset to zero.
@@ -1609,6 +1612,29 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
     const int mw = a.mw;
     const unsigned long long total = a.tprefix[a.nps];
     unsigned long long scanned = 0;
+    // Forward counts of the current (parent, source) slot, summed per tuple in
+    // shared memory when the tuple space is small; flushed to the global
+    // counts when the warp moves to another slot and at the end.
+    __shared__ unsigned long long sweep_acc[8][kSweepAccKeys];
+    unsigned long long* const wacc = sweep_acc[threadIdx.x >> 5];
+    const bool use_acc = K <= kSweepAccKeys && (blockDim.x >> 5) <= 8;
+    unsigned long long* acc_cnt = nullptr;   // global counts the accumulator belongs to
+    if (use_acc) {
+        for (int q = lane; q < kSweepAccKeys; q += 32) wacc[q] = 0;
+        __syncwarp();
+    }
+    auto flush = [&]() {
+        if (!acc_cnt) return;
+        __syncwarp();
+        for (int q = lane; q < K; q += 32) {
+            const unsigned long long v = wacc[q];
+            if (v) {
+                atomicAdd(acc_cnt + q, v);
+                wacc[q] = 0;
+            }
+        }
+        __syncwarp();
+    };
     for (unsigned long long task = warp; task < total; task += nwarps) {
         int32_t lo = 0, hi = a.nps - 1;
         while (lo < hi) {
@@ -1635,6 +1661,10 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
         uint32_t* NM = a.M + P.m_off + ((int64_t)s * (P.nv + 1) + P.nv) * P.nloc * mw;
         const int64_t nm_out = P.sz_off + (int64_t)s * K * (P.nv + 1) + P.nv;
         unsigned long long* cnt = a.counts + P.key_base + (int64_t)s * K;
+        if (use_acc && cnt != acc_cnt) {
+            flush();
+            acc_cnt = cnt;
+        }
         scanned += (unsigned long long)(e - st);
         for (int32_t base = st; base < e; base += 32) {
             const int32_t i = base + lane;
@@ -1661,7 +1691,12 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
                 if (lane >= d && uk == segk) v += uv;
             }
             const int32_t nk = __shfl_down_sync(kFull, segk, 1);
-            if (ok && (lane == 31 || nk != segk) && v) atomicAdd(cnt + kc, v);
+            if (ok && (lane == 31 || nk != segk) && v) {
+                if (use_acc)
+                    atomicAdd(wacc + kc, v);
+                else
+                    atomicAdd(cnt + kc, v);
+            }
             const bool fresh = ok && diff > 0 && or_fresh(NM + (int64_t)(to - P.vbase) * mw + (kc >> 5), 1u << (kc & 31));
             const unsigned fmask = __ballot_sync(kFull, fresh);
             if (fresh) {
@@ -1673,6 +1708,7 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
         __syncwarp();
         if (lane == 0) *Ru = 0u;
     }
+    flush();
     // `scanned` is the same in every lane of the warp.
     if (lane == 0 && scanned) atomicAdd(a.scanned, scanned);
 }
