@@ -938,6 +938,11 @@ struct MaskDev {
     int32_t gen_vs, gen_es;      // shared-memory strides of generated rows (odd)
 };
 
+// Tuples per source up to which the sweep sums forward counts per warp in
+// shared memory and counts the source vertex's own domains (the row pass then
+// leaves those domains out).
+constexpr int kSweepAccKeys = 64;
+
 // OR `bits` into *p and return the bits that were not set before (a word
 // already holding all of them costs one L2 read and no atomic).
 __device__ __forceinline__ uint32_t or_fresh(uint32_t* p, uint32_t bits)
@@ -1317,6 +1322,9 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
         for (int w = 0; w < MW; ++w)
             mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
         }
+        // The source vertex's own domain is counted by the sweep when the
+        // tuple space is small (see k_mask_sweep); the other vertices' here.
+        const int skip_p = K <= kSweepAccKeys ? P.src_v[s] : -1;
         if (mw == 1 && nv <= kMaskBatch) {
             // One mask word per vertex: read every vertex's word first, so
             // the L2 round trips overlap, then OR where bits are missing.
@@ -1324,16 +1332,18 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
             uint32_t cur[kMaskBatch];
 #pragma unroll
             for (int p = 0; p < kMaskBatch; ++p)
-                cur[p] = p < nv && mk[0] ? __ldcg(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase)) : ~0u;
+                cur[p] = p < nv && p != skip_p && mk[0] ? __ldcg(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase)) : ~0u;
 #pragma unroll
             for (int p = 0; p < kMaskBatch; ++p) {
                 if (p >= nv) break;
+                if (p == skip_p) continue;
                 const uint32_t fresh =
                     (mk[0] & ~cur[p]) ? mk[0] & ~atomicOr(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase), mk[0]) : 0u;
                 add_fresh_bits(fresh, a.sizes, P.sz_off + (int64_t)s * K * (nv + 1) + p, nv + 1, 0, lane);
             }
         } else {
             for (int p = 0; p < nv; ++p) {
+                if (p == skip_p) continue;
                 uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * P.nloc + (live ? img[p] - P.vbase : 0)) * mw;
                 const int64_t out = P.sz_off + (int64_t)s * K * (nv + 1) + p;
                 for (int w = 0; w < mw; ++w) add_fresh_bits(or_fresh(rowm + w, mk[w]), a.sizes, out, nv + 1, w, lane);
@@ -1597,9 +1607,6 @@ __global__ void k_mask_prefix(int32_t nps, const uint32_t* __restrict__ tcount, 
     tprefix[nps] = run;
 }
 
-// Tuples per source whose forward counts a sweep warp sums in shared memory.
-constexpr int kSweepAccKeys = 64;
-
 // Sweep: warp per touched (parent, source, vertex u) over u's entries in the
 // source's range: child counts by tuple and the new vertex's domain masks.
 // R[u] and the H entries it reads are reset to zero.
@@ -1615,12 +1622,24 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
     // Forward counts of the current (parent, source) slot, summed per tuple in
     // shared memory when the tuple space is small; flushed to the global
     // counts when the warp moves to another slot and at the end.
+    // With the same small tuple space, the source vertex's own domain for
+    // tuple c: every touched u with some entry e of seg(u, c) where
+    // R[u] > H[e], i.e. some row with source image u has a child in c
+    // (exactly the rows whose mask would have included c).  Counted per key
+    // in shared memory (lane q owns keys q and q + 32), flushed with the counts.
     __shared__ unsigned long long sweep_acc[8][kSweepAccKeys];
+    __shared__ uint32_t sweep_src[8][kSweepAccKeys];
     unsigned long long* const wacc = sweep_acc[threadIdx.x >> 5];
+    uint32_t* const wsrc = sweep_src[threadIdx.x >> 5];
     const bool use_acc = K <= kSweepAccKeys && (blockDim.x >> 5) <= 8;
     unsigned long long* acc_cnt = nullptr;   // global counts the accumulator belongs to
+    int64_t acc_src = 0;                     // sizes index of the source domain of key 0
+    int32_t acc_stride = 0;
     if (use_acc) {
-        for (int q = lane; q < kSweepAccKeys; q += 32) wacc[q] = 0;
+        for (int q = lane; q < kSweepAccKeys; q += 32) {
+            wacc[q] = 0;
+            wsrc[q] = 0;
+        }
         __syncwarp();
     }
     auto flush = [&]() {
@@ -1631,6 +1650,11 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
             if (v) {
                 atomicAdd(acc_cnt + q, v);
                 wacc[q] = 0;
+            }
+            const uint32_t d = wsrc[q];
+            if (d) {
+                atomicAdd(a.sizes + acc_src + (int64_t)q * acc_stride, d);
+                wsrc[q] = 0;
             }
         }
         __syncwarp();
@@ -1664,7 +1688,10 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
         if (use_acc && cnt != acc_cnt) {
             flush();
             acc_cnt = cnt;
+            acc_src = P.sz_off + (int64_t)s * K * (P.nv + 1) + P.src_v[s];
+            acc_stride = P.nv + 1;
         }
+        uint32_t child0 = 0, child1 = 0;   // keys c < 32 / c >= 32 where u's rows have a child
         scanned += (unsigned long long)(e - st);
         for (int32_t base = st; base < e; base += 32) {
             const int32_t i = base + lane;
@@ -1697,6 +1724,11 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
                 else
                     atomicAdd(cnt + kc, v);
             }
+            if (use_acc) {
+                const bool child = ok && diff > 0;
+                child0 |= __reduce_or_sync(kFull, child && kc < 32 ? 1u << kc : 0u);
+                child1 |= __reduce_or_sync(kFull, child && kc >= 32 ? 1u << (kc - 32) : 0u);
+            }
             const bool fresh = ok && diff > 0 && or_fresh(NM + (int64_t)(to - P.vbase) * mw + (kc >> 5), 1u << (kc & 31));
             const unsigned fmask = __ballot_sync(kFull, fresh);
             if (fresh) {
@@ -1704,6 +1736,10 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
                 if (lane == __ffs(peers) - 1)
                     atomicAdd(a.sizes + nm_out + (int64_t)kc * (P.nv + 1), (uint32_t)__popc(peers));
             }
+        }
+        if (use_acc) {
+            wsrc[lane] += (child0 >> lane) & 1u;
+            wsrc[lane + 32] += (child1 >> lane) & 1u;
         }
         __syncwarp();
         if (lane == 0) *Ru = 0u;
