@@ -1625,12 +1625,17 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
     // With the same small tuple space, the source vertex's own domain for
     // tuple c: every touched u with some entry e of seg(u, c) where
     // R[u] > H[e], i.e. some row with source image u has a child in c
-    // (exactly the rows whose mask would have included c).  Counted per key
-    // in shared memory (lane q owns keys q and q + 32), flushed with the counts.
+    // (exactly the rows whose mask would have included c).  R - H >= 0 for
+    // every entry, so a run of equal keys has a child exactly when its sum is
+    // positive: the lane that ends the run flags the key (wflag), and at the
+    // end of the task lane q moves the flags of keys q and q + 32 into the
+    // per-key counts (wsrc), flushed with the forward counts.
     __shared__ unsigned long long sweep_acc[8][kSweepAccKeys];
     __shared__ uint32_t sweep_src[8][kSweepAccKeys];
+    __shared__ uint32_t sweep_flag[8][kSweepAccKeys];
     unsigned long long* const wacc = sweep_acc[threadIdx.x >> 5];
     uint32_t* const wsrc = sweep_src[threadIdx.x >> 5];
+    uint32_t* const wflag = sweep_flag[threadIdx.x >> 5];
     const bool use_acc = K <= kSweepAccKeys && (blockDim.x >> 5) <= 8;
     unsigned long long* acc_cnt = nullptr;   // global counts the accumulator belongs to
     int64_t acc_src = 0;                     // sizes index of the source domain of key 0
@@ -1639,6 +1644,7 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
         for (int q = lane; q < kSweepAccKeys; q += 32) {
             wacc[q] = 0;
             wsrc[q] = 0;
+            wflag[q] = 0;
         }
         __syncwarp();
     }
@@ -1691,7 +1697,6 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
             acc_src = P.sz_off + (int64_t)s * K * (P.nv + 1) + P.src_v[s];
             acc_stride = P.nv + 1;
         }
-        uint32_t child0 = 0, child1 = 0;   // keys c < 32 / c >= 32 where u's rows have a child
         scanned += (unsigned long long)(e - st);
         for (int32_t base = st; base < e; base += 32) {
             const int32_t i = base + lane;
@@ -1719,15 +1724,12 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
             }
             const int32_t nk = __shfl_down_sync(kFull, segk, 1);
             if (ok && (lane == 31 || nk != segk) && v) {
-                if (use_acc)
+                if (use_acc) {
                     atomicAdd(wacc + kc, v);
-                else
+                    wflag[kc] = 1u;
+                } else {
                     atomicAdd(cnt + kc, v);
-            }
-            if (use_acc) {
-                const bool child = ok && diff > 0;
-                child0 |= __reduce_or_sync(kFull, child && kc < 32 ? 1u << kc : 0u);
-                child1 |= __reduce_or_sync(kFull, child && kc >= 32 ? 1u << (kc - 32) : 0u);
+                }
             }
             const bool fresh = ok && diff > 0 && or_fresh(NM + (int64_t)(to - P.vbase) * mw + (kc >> 5), 1u << (kc & 31));
             const unsigned fmask = __ballot_sync(kFull, fresh);
@@ -1737,9 +1739,12 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
                     atomicAdd(a.sizes + nm_out + (int64_t)kc * (P.nv + 1), (uint32_t)__popc(peers));
             }
         }
+        __syncwarp();
         if (use_acc) {
-            wsrc[lane] += (child0 >> lane) & 1u;
-            wsrc[lane + 32] += (child1 >> lane) & 1u;
+            wsrc[lane] += wflag[lane];
+            wsrc[lane + 32] += wflag[lane + 32];
+            wflag[lane] = 0u;
+            wflag[lane + 32] = 0u;
         }
         __syncwarp();
         if (lane == 0) *Ru = 0u;
