@@ -419,6 +419,8 @@ def gpu_arm(args, wl) -> None:
                                "domain sizes": sum(s["domain_ms"] for s in stats) / len(stats)},
         "paths": {"mask_parents": stats[-1]["mask_parents"], "candidate_parents": stats[-1]["candidate_parents"]},
         "fused_rows_per_step": stats[-1]["fused_rows"],
+        "host_ms_per_step": {"mine_call": statistics.median(s["mine_ms"] for s in stats),
+                             "blocked_in_sync": statistics.median(s["sync_ms"] for s in stats)},
         "pruned": {"vertices": stats[-1]["pruned_vertices"], "entries": stats[-1]["pruned_entries"]},
     }
     print(json.dumps(line), flush=True)

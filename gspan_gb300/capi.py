@@ -67,7 +67,7 @@ class Stats(ctypes.Structure):
                 ("seed_ms", ctypes.c_double), ("domain_ms", ctypes.c_double),
                 ("canonical_checks", ctypes.c_uint64), ("canonical_ms", ctypes.c_double),
                 ("pruned_vertices", ctypes.c_uint64), ("pruned_entries", ctypes.c_uint64),
-                ("fused_rows", ctypes.c_uint64)]
+                ("fused_rows", ctypes.c_uint64), ("sync_ms", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

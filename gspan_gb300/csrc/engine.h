@@ -36,6 +36,7 @@ enum : uint32_t {
     kErrAsymmetric = 1u << 3,   // upload: an entry without its reverse entry (not an error)
     kFlagParallel = 1u << 4,    // upload: two equal entries of one vertex (parallel edges; not an error)
     kFlagSelfLoop = 1u << 5,    // upload: some vertex has an entry to itself (not an error)
+    kErrCounter = 1u << 6,      // a 32-bit per-vertex row counter (R) of the mask path would wrap
 };
 
 // The graph in HBM.  Labels are replaced by their rank among the distinct
@@ -104,6 +105,11 @@ struct DevGraph {
 // lane).  Fewer rows give the tile queue more, lighter units to balance when
 // some rows' frequent segments are long (hubs).
 constexpr int kMatTileRows = 8;
+
+// Tuples per source (nel * lwin) up to which the sweep sums forward counts
+// per warp in shared memory and counts the source vertex's own domains (the
+// row pass then leaves those domains out of M).
+constexpr int kSweepAccKeys = 64;
 
 // Widest per-vertex key mask the mask kernels handle (x 32 keys).
 constexpr int kMaxMaskWords = 16;

@@ -938,11 +938,6 @@ struct MaskDev {
     int32_t gen_vs, gen_es;      // shared-memory strides of generated rows (odd)
 };
 
-// Tuples per source up to which the sweep sums forward counts per warp in
-// shared memory and counts the source vertex's own domains (the row pass then
-// leaves those domains out).
-constexpr int kSweepAccKeys = 64;
-
 // OR `bits` into *p and return the bits that were not set before (a word
 // already holding all of them costs one L2 read and no atomic).
 __device__ __forceinline__ uint32_t or_fresh(uint32_t* p, uint32_t bits)
@@ -1137,8 +1132,13 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
         bool first_row = false;   // this lane's group made R[u] non-zero
         if (live) {
             const unsigned peers = __match_any_sync(lm, u);
-            if (lane == __ffs(peers) - 1)
-                first_row = atomicAdd(a.R + P.r_off + (int64_t)s * P.nloc + (u - P.vbase), (uint32_t)__popc(peers)) == 0;
+            if (lane == __ffs(peers) - 1) {
+                const uint32_t add = (uint32_t)__popc(peers);
+                const uint32_t before = atomicAdd(a.R + P.r_off + (int64_t)s * P.nloc + (u - P.vbase), add);
+                first_row = before == 0;
+                // R (and H <= R) are 32-bit: a wrap would corrupt counts, so it fails the job.
+                if (before > 0xFFFFFFFFu - add) atomicOr(a.status, kErrCounter);
+            }
         }
         // One append per warp for the source images seen for the first time.
         const unsigned fm = __ballot_sync(kFull, first_row);

@@ -255,6 +255,15 @@ struct Run {
     cudaStream_t s;
     bool profile;
 
+    // A stream synchronisation, its blocked host time summed into the stats.
+    cudaError_t wait(cudaStream_t strm)
+    {
+        const auto w0 = Clock::now();
+        const cudaError_t e = cudaStreamSynchronize(strm);
+        st.sync_ms += std::chrono::duration<double, std::milli>(Clock::now() - w0).count();
+        return e;
+    }
+
     // Every host<->device copy of a mining run goes through here and is counted.
     cudaError_t copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t strm)
     {
@@ -365,7 +374,7 @@ struct Run {
         GS_CK(copy(h.data(), d_sizes, h.size() * 4, cudaMemcpyDeviceToHost, s), "read sizes");
         uint32_t status = 0;
         GS_CK(copy(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
-        GS_CK(cudaStreamSynchronize(s), "domain sizes");
+        GS_CK(wait(s), "domain sizes");
         dfree(d_sizes, s);
         if (profile) {
             float ms = 0;
@@ -398,7 +407,7 @@ struct Run {
         ++st.kernel_launches;
         std::vector<unsigned long long> counts((size_t)nkeys);
         GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read seed counts");
-        GS_CK(cudaStreamSynchronize(s), "seed count");
+        GS_CK(wait(s), "seed count");
         std::vector<Active> act;
         for (int64_t key = 0; key < nkeys; ++key) {
             const uint64_t c = counts[key];
@@ -720,7 +729,10 @@ struct Run {
             sz_off[i] = sz_total;
             sz_total += (int64_t)P.nsrc * K * (P.nv + 1) + (int64_t)P.nback * g.nel * P.nv;
             G.bytes += bytes;
-            rows_bytes += (double)rows * (4.0 * P.nv + P.nsrc * (16.0 + 4.0 * g.segw + 4.0 * P.nv * g.segw) +
+            // Mask ORs for the pattern vertices other than the source when
+            // the sweep counts the source's own domain.
+            const int mvert = K <= kSweepAccKeys ? P.nv - 1 : P.nv;
+            rows_bytes += (double)rows * (4.0 * P.nv + P.nsrc * (16.0 + 4.0 * g.segw + 4.0 * mvert * g.segw) +
                                           8.0 * P.nback);
             G.metas.push_back(P);
         }
@@ -893,7 +905,7 @@ struct Run {
         if (sz_total) GS_CK(copy(sizes.data(), d_sizes, sz_total * 4, cudaMemcpyDeviceToHost, s), "read sizes");
         GS_CK(copy(ctr, ctx->d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s), "read counters");
         GS_CK(copy(&mstat, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
-        GS_CK(cudaStreamSynchronize(s), "extension count");
+        GS_CK(wait(s), "extension count");
         resolve();
         settle();
         st.scanned_entries += ctr[1] + ctr[3];
@@ -1195,7 +1207,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<in
         cudaStreamSynchronize(run.s);
         return rc;
     }
-    GS_CK(cudaStreamSynchronize(run.s), "mine");
+    GS_CK(run.wait(run.s), "mine");
     run.settle();
 
     std::sort(run.found.begin(), run.found.end(),

@@ -115,6 +115,8 @@ typedef struct gspan_stats {
     uint64_t pruned_entries;     /* opts.prune: directed entries dropped with them */
     uint64_t fused_rows;         /* next-to-last-level embeddings generated inside the last level's row pass
                                     instead of being stored */
+    double sync_ms;              /* host time blocked in stream synchronisations (the rest of mine_ms is host
+                                    work and launch calls) */
 } gspan_stats;
 
 typedef struct gspan_ctx gspan_ctx;
