@@ -34,9 +34,14 @@ to add up to the whole job's.
 --workload serving: a Poisson stream (mean --rate jobs/s) of jobs over
 resident graphs of the three single-graph sizes; jobs/s with p50/p95/p99
 latency, each result checked against the same job run alone.
---workload batch_256: the batched engine against the plain one.
---workload chung_lu_3_7m / chung_lu_3_7m_k4 / chung_lu_100k_wide: other
-single-graph jobs (the large graph at 3 and 4 edges; a wide label space).
+--workload batch_256: the batched engine against the plain one (k 3 by
+default; --batch-k 4 runs the stated size, minutes per job).
+--workload chung_lu_3_7m / chung_lu_3_7m_k4 / chung_lu_3_7m_k4_s20k /
+chung_lu_100k_wide: other single-graph jobs (the large graph at 3 edges, at
+4 edges with support 100,000, at 4 edges with its stated support 20,000 -
+minutes per job, its 3-edge level generated rather than stored - and a wide
+label space).
+--fused-last 0|1|2 and --prune set the miner's options of the same names.
 --workload text_load: loading a graph from gSpan text on the device against
 the host reader and upload.
 
