@@ -984,44 +984,17 @@ __global__ void k_segments(int32_t n, int32_t m, int32_t lwin, int32_t K, int32_
         if (b < 0 || e < b || e > m) continue;   // malformed range (rejected by the upload)
         auto key = [&](int32_t j) { return (int32_t)(entry_el(adj[j]) * (uint32_t)lwin + entry_tl(adj[j])) - wb; };
         int32_t* out = segstart ? segstart + v * (int64_t)(K + 1) : nullptr;
-        // The warp owns the vertex: with one or two mask words its bits are
-        // ORed across lanes in registers and each word is stored once.
-        const bool few = segw <= 2;
-        uint32_t m0 = 0, m1 = 0, o0 = 0, o1 = 0;
-        for (int32_t base = b; base < e; base += 32) {
-            const int32_t j = base + lane;
-            uint32_t bit = 0, one = 0;
-            int32_t kc = -1;
-            if (j < e) {
-                kc = key(j);
-                const int32_t kp = j > b ? key(j - 1) : -1;
-                if (kp < kc && kc >= 0 && kc < 32 * segw) {
-                    bit = 1u << (kc & 31);
-                    one = (j + 1 == e || key(j + 1) > kc) ? bit : 0u;
-                    if (!few) {
-                        const int64_t w = v * segw + (kc >> 5);
-                        atomicOr(segmask + w, bit);
-                        if (one) atomicOr(segone + w, bit);
-                    }
-                }
-                if (out)
-                    for (int32_t k = kp + 1; k <= kc && k <= K; ++k) out[k] = j;
+        for (int32_t j = b + lane; j < e; j += 32) {
+            const int32_t kc = key(j);
+            const int32_t kp = j > b ? key(j - 1) : -1;
+            if (kp < kc && kc >= 0 && kc < 32 * segw) {
+                const int64_t w = v * segw + (kc >> 5);
+                const uint32_t bit = 1u << (kc & 31);
+                atomicOr(segmask + w, bit);
+                if (j + 1 == e || key(j + 1) > kc) atomicOr(segone + w, bit);
             }
-            if (few) {
-                const bool hi = kc >= 32;
-                m0 |= __reduce_or_sync(kFull, hi ? 0u : bit);
-                o0 |= __reduce_or_sync(kFull, hi ? 0u : one);
-                m1 |= __reduce_or_sync(kFull, hi ? bit : 0u);
-                o1 |= __reduce_or_sync(kFull, hi ? one : 0u);
-            }
-        }
-        if (few && lane == 0) {
-            segmask[v * segw] = m0;
-            segone[v * segw] = o0;
-            if (segw == 2) {
-                segmask[v * segw + 1] = m1;
-                segone[v * segw + 1] = o1;
-            }
+            if (out)
+                for (int32_t k = kp + 1; k <= kc && k <= K; ++k) out[k] = j;
         }
         if (out) {
             const int32_t kl = e > b ? key(e - 1) : -1;
