@@ -211,6 +211,9 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
     const int64_t erange = M > 0 ? (int64_t)mm[3] - mm[2] + 1 : 0;
     const int32_t elo = mm[2];
     bool dense = vrange <= kDenseRange && erange <= kDenseRange;
+    // Host sources of copies still in flight: they live until the upload's
+    // status sync below (every early return syncs the stream first).
+    std::vector<int32_t> vtab, etab, vrank;
     if (dense) {
         std::vector<uint8_t> vflag((size_t)vrange), eflag((size_t)erange);
         if (vrange) UP_CK(cudaMallocAsync(&d_vflag, (size_t)vrange, s), "alloc flags");
@@ -221,7 +224,8 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         if (vrange) UP_CK(cudaMemcpyAsync(vflag.data(), d_vflag, (size_t)vrange, cudaMemcpyDeviceToHost, s), "flags");
         if (erange) UP_CK(cudaMemcpyAsync(eflag.data(), d_eflag, (size_t)erange, cudaMemcpyDeviceToHost, s), "flags");
         UP_CK(cudaStreamSynchronize(s), "label presence");
-        std::vector<int32_t> vtab((size_t)vrange, -1), etab((size_t)erange, -1);
+        vtab.assign((size_t)vrange, -1);
+        etab.assign((size_t)erange, -1);
         for (int64_t v = 0; v < vrange; ++v)
             if (vflag[(size_t)v]) {
                 vtab[(size_t)v] = (int32_t)g.vlabel_of_rank.size();
@@ -241,7 +245,6 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
             UP_CK(cudaMallocAsync(&d_etab, (size_t)erange * 4, s), "alloc rank table");
             UP_CK(cudaMemcpyAsync(d_etab, etab.data(), (size_t)erange * 4, cudaMemcpyHostToDevice, s), "rank table");
         }
-        UP_CK(cudaStreamSynchronize(s), "rank tables");   // host tables leave scope
     } else {
         // Sparse label values: rank on the host.
         if (on_device) {
@@ -268,7 +271,6 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         dist.erase(std::unique(dist.begin(), dist.end()), dist.end());
         g.elabel_of_rank = dist;
         if (nv_dev > 0) {
-            std::vector<int32_t> vrank;
             rank_labels(vls[0], (size_t)N, 1, g.vlabel_of_rank, &vrank);
             UP_CK(cudaMemcpyAsync(g.vrank, vrank.data(), (size_t)N * 4, cudaMemcpyHostToDevice, s), "copy vrank");
         }
@@ -278,13 +280,12 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
                                   cudaMemcpyHostToDevice, s),
                   "copy edge labels");
         }
-        UP_CK(cudaStreamSynchronize(s), "host ranks");
     }
     if (ninst == 1) {
         g.lwin = (int32_t)g.vlabel_of_rank.size();
         g.win_base_h.assign(g.vlabel_of_rank.size(), 0);
     } else {
-        std::vector<int32_t> vrank((size_t)N);
+        vrank.assign((size_t)N, 0);
         for (int32_t i = 0; i < ninst; ++i) {
             std::vector<int32_t> distinct, local;
             rank_labels(vls[i], (size_t)ns[i], 1, distinct, &local);
@@ -299,7 +300,6 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         }
         if (N > 0)
             UP_CK(cudaMemcpyAsync(g.vrank, vrank.data(), (size_t)N * 4, cudaMemcpyHostToDevice, s), "copy vrank");
-        UP_CK(cudaStreamSynchronize(s), "batch ranks");
     }
     g.inst_vbase = vbase;
     g.inst_ebase = ebase;
