@@ -1118,6 +1118,15 @@ struct BackAcc {
     }
 };
 
+// Bit of the unordered pattern-vertex pair {i, j} in a 32-bit set; a vertex
+// paired with itself (a self-loop query) and pairs with a vertex beyond the
+// eighth have none.
+__device__ __forceinline__ uint32_t pair_bit(int i, int j)
+{
+    const int lo = min(i, j), hi = max(i, j);
+    return hi < 8 && lo != hi ? 1u << (hi * (hi - 1) / 2 + lo) : 0u;
+}
+
 template <int MW, class Ecol>
 __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, const int32_t* img, const Ecol& ecol,
                                          bool live, int lane, BackAcc& acc)
@@ -1126,6 +1135,11 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
     const int mw = a.mw;
     const int nv = P.nv, nsrc = P.nsrc;
     const int min_label = P.min_label;
+    // Pairs of the row's images found not adjacent through the edge index
+    // (one edge label, symmetric graph: the entry-column case), so a pair
+    // probed from one source is not probed again from the other end or as a
+    // backward target.
+    uint32_t absent = 0;
     for (int s = 0; s < nsrc; ++s) {
         const int32_t u = live ? img[P.src_v[s]] : -1;
         const unsigned lm = __ballot_sync(kFull, live);
@@ -1228,8 +1242,13 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
                 if (pos < 0) {
                     if (x == u && !((__ldg(a.selfloop + (u >> 5)) >> (u & 31)) & 1u)) continue;
                     if (a.eidx) {
+                        const uint32_t pb = pair_bit(vs, j);
+                        if (absent & pb) continue;
                         pos = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)u, key);
-                        if (pos < 0) continue;
+                        if (pos < 0) {
+                            absent |= pb;
+                            continue;
+                        }
                     } else {
                         if (x != u && jj < 0 && a.symmetric) {
                             const int32_t xb = __ldg(a.offsets + x), xe = __ldg(a.offsets + x + 1);
@@ -1364,7 +1383,9 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
                 const uint64_t want = pack_entry((uint32_t)el, tlx, (uint32_t)x);
                 int32_t pos;
                 if (a.eidx) {
-                    pos = edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)un, want);
+                    pos = a.ecol >= 0 && (absent & pair_bit(P.vn, bv))
+                              ? -1
+                              : edge_find(a.eidx, a.eidx_cap, a.adj, b, e, (uint32_t)un, want);
                 } else {
                     pos = lower_bound_entry(a.adj, b, e, want);
                     if (pos >= e || __ldg(a.adj + pos) != want) pos = -1;
