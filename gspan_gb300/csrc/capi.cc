@@ -116,6 +116,10 @@ void gspan_ctx_destroy(gspan_ctx* ctx)
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     for (cudaEvent_t ev : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d})
         if (ev) cudaEventDestroy(ev);
+    for (auto& p : ctx->ev_pool) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

@@ -304,4 +304,27 @@ cudaError_t launch_mask_gen(const MaskArgs& a, cudaStream_t st);
 // Prefix of the touched lists, then the sweep (two launches).
 cudaError_t launch_mask_sweep(const MaskArgs& a, cudaStream_t st);
 
+// Several buffers set to one 32-bit value each, in one launch instead of a
+// memset per buffer (each memset is an API call and a stream operation of
+// its own).  Spans with no words are skipped.
+constexpr int kMaxClearSpans = 12;
+struct ClearSpan {
+    void* p;
+    int64_t words;    // 32-bit words
+    uint32_t value;
+};
+struct ClearList {
+    ClearSpan span[kMaxClearSpans];
+    int n = 0;
+    // Adds a span; false when the list is full.
+    bool add(void* p, int64_t words, uint32_t value = 0)
+    {
+        if (!p || words <= 0) return true;
+        if (n == kMaxClearSpans) return false;
+        span[n++] = ClearSpan{p, words, value};
+        return true;
+    }
+};
+cudaError_t launch_clear(const ClearList& l, cudaStream_t st);
+
 }  // namespace gs

@@ -2082,6 +2082,39 @@ cudaError_t launch_mask_gen(const MaskArgs& x, cudaStream_t st)
     return cudaGetLastError();
 }
 
+namespace {
+// blockIdx.y picks the span; 16-byte stores where the span is 16-byte
+// aligned (stream-ordered allocations are), 4-byte stores for the rest.
+__global__ void k_clear(ClearList l)
+{
+    const ClearSpan sp = l.span[blockIdx.y];
+    uint32_t* p = static_cast<uint32_t*>(sp.p);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t head = 0;
+    if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+        const int64_t n4 = sp.words >> 2;
+        const uint4 v = make_uint4(sp.value, sp.value, sp.value, sp.value);
+        uint4* p4 = reinterpret_cast<uint4*>(p);
+        for (int64_t i = t; i < n4; i += stride) p4[i] = v;
+        head = n4 << 2;
+    }
+    for (int64_t i = head + t; i < sp.words; i += stride) p[i] = sp.value;
+}
+}  // namespace
+
+cudaError_t launch_clear(const ClearList& l, cudaStream_t st)
+{
+    if (l.n == 0) return cudaSuccess;
+    int64_t most = 0;
+    for (int i = 0; i < l.n; ++i) most = std::max(most, l.span[i].words);
+    const int64_t want = (most / 4 + 255) / 256;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    const int gx = (int)std::max<int64_t>(1, std::min(want, cap));
+    k_clear<<<dim3(gx, l.n), 256, 0, st>>>(l);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_mask_sweep(const MaskArgs& x, cudaStream_t st)
 {
     if (x.nps == 0) return cudaSuccess;

@@ -255,6 +255,17 @@ struct Run {
     cudaStream_t s;
     bool profile;
 
+    // Free device memory for the size decisions (group budgets, stored or
+    // generated last levels).  The query costs tens of microseconds, so it is
+    // taken while kernels run - after the seed count and each level's launches -
+    // and the decisions use the latest value.
+    size_t free_b = 0;
+    void refresh_free()
+    {
+        size_t f = 0, t = 0;
+        if (cudaMemGetInfo(&f, &t) == cudaSuccess) free_b = f;
+    }
+
     // A stream synchronisation, its blocked host time summed into the stats.
     cudaError_t wait(cudaStream_t strm)
     {
@@ -327,9 +338,6 @@ struct Run {
         GS_CK(copy(as.d_act, act_h.data(), act_h.size() * 4, cudaMemcpyHostToDevice, s), "copy act");
         if (as.nact > 0) {
             GS_CK(dalloc(&as.pool, bitmap_words + hash_words, s), "alloc domains");
-            if (bitmap_words) GS_CK(cudaMemsetAsync(as.pool, 0, bitmap_words * 4, s), "clear bitmaps");
-            if (hash_words)
-                GS_CK(cudaMemsetAsync(as.pool + bitmap_words, 0xFF, hash_words * 4, s), "clear hashsets");
             GS_CK(dalloc(&as.d_dom, act.size(), s), "alloc dom");
             GS_CK(copy(as.d_dom, as.dom.data(), act.size() * sizeof(DomDesc), cudaMemcpyHostToDevice, s),
                   "copy dom");
@@ -337,7 +345,12 @@ struct Run {
             GS_CK(copy(as.d_mat, as.mat.data(), act.size() * sizeof(long long), cudaMemcpyHostToDevice, s),
                   "copy mat");
             GS_CK(dalloc(&as.d_cursor, act.size(), s), "alloc cursor");
-            GS_CK(cudaMemsetAsync(as.d_cursor, 0, act.size() * 8, s), "clear cursor");
+            // Bitmaps zero, hashsets empty (~0), cursors zero: one launch.
+            ClearList aclr;
+            aclr.add(as.pool, (int64_t)bitmap_words);
+            aclr.add(as.pool + bitmap_words, (int64_t)hash_words, 0xFFFFFFFFu);
+            aclr.add(as.d_cursor, (int64_t)act.size() * 2);
+            GS_CK(launch_clear(aclr, s), "clear launch");
         }
         if (materialize && out_rows > 0) {
             // One entry column (the seed's entry) follows the vertex columns.
@@ -405,6 +418,7 @@ struct Run {
         if (profile) cudaEventRecord(ctx->ev_a, s);
         GS_CK(launch_seed_count(g, d_counts, s), "seed count launch");
         ++st.kernel_launches;
+        refresh_free();
         std::vector<unsigned long long> counts((size_t)nkeys);
         GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read seed counts");
         GS_CK(wait(s), "seed count");
@@ -485,13 +499,12 @@ struct Run {
         }
         ev_pending.clear();
     }
+    // The event pairs go back to the context for its next run (creating and
+    // destroying them took tens of microseconds per run).
     void drop_events()
     {
         resolve();
-        for (auto& p : ev_free) {
-            cudaEventDestroy(p.first);
-            cudaEventDestroy(p.second);
-        }
+        ctx->ev_pool.insert(ctx->ev_pool.end(), ev_free.begin(), ev_free.end());
         ev_free.clear();
     }
 
@@ -520,8 +533,6 @@ struct Run {
             bytes += 4.0 * ncols * (double)f.count;
         }
         if (mode == 2) return true;
-        size_t free_b = 0, total_b = 0;
-        cudaMemGetInfo(&free_b, &total_b);
         return bytes > 0.5 * (double)free_b;
     }
 
@@ -677,8 +688,6 @@ struct Run {
         std::vector<int64_t> sz_off(np, -1);
         int64_t ctiles = 0, atiles = 0, sz_total = 0;
         double rows_bytes = 0, cand_read_bytes = 0, all_read_bytes = 0;
-        size_t free_b = 0, total_b = 0;
-        cudaMemGetInfo(&free_b, &total_b);
         // The mask groups may hold this share of the free device memory.
         const double share = ctx->opts.mem_fraction > 0 ? std::min(0.4, ctx->opts.mem_fraction) : 0.4;
         const double budget = std::max(2.5e8, share * (double)free_b);
@@ -769,8 +778,10 @@ struct Run {
         } guard{release};
 
         GS_CK(dalloc(&d_counts, (size_t)nkeys, s), "alloc counts");
-        GS_CK(cudaMemsetAsync(d_counts, 0, nkeys * 8, s), "clear counts");
-        GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), s), "clear counters");
+        // Everything the level's first launch needs zeroed, cleared in one launch.
+        ClearList clr;
+        clr.add(d_counts, nkeys * 2);
+        clr.add(ctx->d_counters, 8);
 
         cudaEvent_t e0, e1;
         int32_t gen_nv = 0;
@@ -802,18 +813,25 @@ struct Run {
             GS_CK(dalloc(&d_psp, (size_t)mps, s), "alloc slot parents");
             GS_CK(dalloc(&d_mg, (size_t)mmeta, s), "alloc mask parents");
             GS_CK(dalloc(&d_sizes, (size_t)std::max<int64_t>(sz_total, 1), s), "alloc sizes");
-            GS_CK(cudaMemsetAsync(d_R, 0, mr * 4, s), "clear R");
-            GS_CK(cudaMemsetAsync(d_H, 0, std::max<int64_t>(mh, 1) * 4, s), "clear H");
-            GS_CK(cudaMemsetAsync(d_sizes, 0, std::max<int64_t>(sz_total, 1) * 4, s), "clear sizes");
-            for (const MGroup& G : groups) {
+            clr.add(d_R, mr);
+            clr.add(d_H, std::max<int64_t>(mh, 1));
+            clr.add(d_sizes, std::max<int64_t>(sz_total, 1));
+            for (size_t gi = 0; gi < groups.size(); ++gi) {
+                const MGroup& G = groups[gi];
                 GS_CK(copy(d_mg, G.metas.data(), G.metas.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s),
                       "copy mask parents");
                 GS_CK(copy(d_psp, G.ps_parent.data(), G.ps_parent.size() * 4, cudaMemcpyHostToDevice, s),
                       "copy slot parents");
-                if (G.m) GS_CK(cudaMemsetAsync(d_M, 0, G.m * 4, s), "clear M");
-                if (G.b) GS_CK(cudaMemsetAsync(d_MB, 0, G.b * 4, s), "clear MB");
-                GS_CK(cudaMemsetAsync(d_tcount, 0, G.ps_parent.size() * 4, s), "clear touched counts");
-                GS_CK(cudaMemsetAsync(ctx->d_counters + 2, 0, 8, s), "clear tile counter");
+                // Per group: its masks, touched counts and tile counter (the
+                // sweep leaves R and H zero); the first group's go with the
+                // level's clears.
+                ClearList gclr;
+                ClearList& c = gi == 0 ? clr : gclr;
+                if (!(c.add(d_M, G.m) && c.add(d_MB, G.b) && c.add(d_tcount, (int64_t)G.ps_parent.size()) &&
+                      c.add(ctx->d_counters + 2, 2)))
+                    return fail(ctx, GSPAN_ERR_CUDA, "clear list full");
+                GS_CK(launch_clear(c, s), "clear launch");
+                c.n = 0;
                 MaskArgs ma{};
                 ma.g = &g;
                 ma.parents = d_mg;
@@ -865,6 +883,7 @@ struct Run {
         x.tile_counter = ctx->d_counters;
         x.scanned = ctx->d_counters + 1;
         x.status = ctx->d_status;
+        GS_CK(launch_clear(clr, s), "clear launch");   // no-op when a mask group took the list
         if (!cg.empty()) {
             GS_CK(dalloc(&d_cg, cg.size(), s), "alloc parents");
             GS_CK(copy(d_cg, cg.data(), cg.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
@@ -878,6 +897,7 @@ struct Run {
             ++st.kernel_launches;
             ++st.expand_launches;
         }
+        refresh_free();
         // A child's code does not depend on its counts: while the GPU
         // counts, test the level's child tuples for minimum codes on the
         // host, stopping as soon as the stream is done so the GPU never
@@ -1071,7 +1091,6 @@ struct Run {
         GS_CK(dalloc(&d_mat, freq.size(), s), "alloc mat");
         GS_CK(copy(d_mat, mat_h.data(), mat_h.size() * sizeof(long long), cudaMemcpyHostToDevice, s), "copy mat");
         GS_CK(dalloc(&d_cur, freq.size(), s), "alloc cursor");
-        GS_CK(cudaMemsetAsync(d_cur, 0, freq.size() * 8, s), "clear cursor");
         // Entry columns (one per pattern edge of the children) follow.
         if (table.ecol >= 0) {
             out.ecol = ncols;
@@ -1111,7 +1130,12 @@ struct Run {
         }
         GS_CK(dalloc(&d_all, all.size(), s), "alloc parents");
         GS_CK(copy(d_all, all.data(), all.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
-        GS_CK(cudaMemsetAsync(ctx->d_counters, 0, 16, s), "clear counters");
+        {
+            ClearList mclr;
+            mclr.add(d_cur, (int64_t)freq.size() * 2);
+            mclr.add(ctx->d_counters, 4);
+            GS_CK(launch_clear(mclr, s), "clear launch");
+        }
         x.parents = d_all;
         x.parents_h = all.data();
         x.nparents = (int32_t)all.size();
@@ -1180,6 +1204,7 @@ gspan_status mine(gspan_ctx* ctx, const DevGraph& g, int k, const std::vector<in
     Run run{ctx, g, k, minsup};
     run.s = ctx->stream;
     run.profile = ctx->opts.profile != 0;
+    run.ev_free.swap(ctx->ev_pool);
     GS_CK(cudaMemsetAsync(ctx->d_status, 0, 4, run.s), "clear status");
 
     std::vector<Parent> parents;
