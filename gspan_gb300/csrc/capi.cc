@@ -114,6 +114,7 @@ void gspan_ctx_destroy(gspan_ctx* ctx)
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     for (cudaEvent_t ev : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d})
         if (ev) cudaEventDestroy(ev);
     for (auto& p : ctx->ev_pool) {

@@ -261,6 +261,20 @@ cudaError_t launch_domain_sizes(const DomDesc* dom, int32_t nact, const uint32_t
 int expand_grid_blocks(int device);
 
 // Mask path.
+// One plane of mask words (M: per parent, source and pattern vertex; MB:
+// per parent and pattern vertex): `words` words per vertex of the parent's
+// window, bit i of a vertex's words counting into sizes[sz_base + i * sz_stride]
+// for i < nbits.
+struct MaskPlane {
+    int64_t off;       // first word in M (mb = 0) or MB (mb = 1)
+    int64_t sz_base;
+    int32_t nloc;
+    int32_t sz_stride;
+    int32_t nbits;
+    int16_t words;
+    int16_t mb;
+};
+
 struct MaskArgs {
     const DevGraph* g;
     const ParentMeta* parents;   // device, one group of mask-path parents
@@ -288,6 +302,10 @@ struct MaskArgs {
     int32_t* const* gen_cols = nullptr;
     int32_t gen_ecol = -1;
     int32_t gen_nv = 0;          // most vertices of any generated row
+    // The group's mask planes, counted into `sizes` after the sweep.
+    const MaskPlane* planes = nullptr;
+    int32_t nplanes = 0;
+    int64_t max_plane_nloc = 0;
 };
 // Segment masks (zeroed by the caller), singleton masks and, when
 // allocated, segment starts, in one pass over each vertex's entries.
@@ -303,6 +321,8 @@ cudaError_t launch_mask_rows(const MaskArgs& a, cudaStream_t st);
 cudaError_t launch_mask_gen(const MaskArgs& a, cudaStream_t st);
 // Prefix of the touched lists, then the sweep (two launches).
 cudaError_t launch_mask_sweep(const MaskArgs& a, cudaStream_t st);
+// Domain sizes of the group's tuples from its mask planes (after the sweep).
+cudaError_t launch_mask_popcount(const MaskArgs& a, cudaStream_t st);
 
 // Several buffers set to one 32-bit value each, in one launch instead of a
 // memset per buffer (each memset is an API call and a stream operation of

@@ -938,31 +938,12 @@ struct MaskDev {
     int32_t gen_vs, gen_es;      // shared-memory strides of generated rows (odd)
 };
 
-// OR `bits` into *p and return the bits that were not set before (a word
-// already holding all of them costs one L2 read and no atomic).
-__device__ __forceinline__ uint32_t or_fresh(uint32_t* p, uint32_t bits)
+// OR `bits` into *p without waiting for the old value (the atomic's result
+// is unused); a word already holding them costs one L2 read and no atomic.
+__device__ __forceinline__ void or_bits(uint32_t* p, uint32_t bits)
 {
-    if (!bits || (__ldcg(p) & bits) == bits) return 0u;
-    return bits & ~atomicOr(p, bits);
+    if (bits && (__ldcg(p) & bits) != bits) atomicOr(p, bits);
 }
-
-// Warp-wide: every bit b newly set by any lane in `word` adds the number of
-// such lanes to its tuple's domain size sizes[out + (word * 32 + b) * stride].
-// `out`, `stride` and `word` are the same in every lane.
-__device__ __forceinline__ void add_fresh_bits(uint32_t fresh, uint32_t* sizes, int64_t out, int32_t stride, int word,
-                                               int lane)
-{
-    if (!__any_sync(kFull, fresh)) return;
-    // An image seen for the first time brings most of its tuple bits at once,
-    // so transpose all 32 bits and let lane b add bit b's count.
-    uint32_t mine = 0;
-    for (int b = 0; b < 32; ++b) {
-        const uint32_t c = __popc(__ballot_sync(kFull, (fresh >> b) & 1u));
-        if (lane == b) mine = c;
-    }
-    if (mine) atomicAdd(sizes + out + (int64_t)(word * 32 + lane) * stride, mine);
-}
-
 
 // Warp per vertex, over its entries (sorted by window key kc): the entry
 // that opens segment kc sets bit kc of segmask, and of segone when it also
@@ -1342,7 +1323,8 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
             mk[w] = w < mw ? (__ldg(a.segmask + (int64_t)u * mw + w) & P.range[s][w] & ~ex[w]) : 0u;
         }
         // The source vertex's own domain is counted by the sweep when the
-        // tuple space is small (see k_mask_sweep); the other vertices' here.
+        // tuple space is small (see k_mask_sweep); the other vertices' masks
+        // are ORed here and counted afterwards (k_mask_popcount).
         const int skip_p = K <= kSweepAccKeys ? P.src_v[s] : -1;
         if (mw == 1 && nv <= kMaskBatch) {
             // One mask word per vertex: read every vertex's word first, so
@@ -1356,16 +1338,13 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
             for (int p = 0; p < kMaskBatch; ++p) {
                 if (p >= nv) break;
                 if (p == skip_p) continue;
-                const uint32_t fresh =
-                    (mk[0] & ~cur[p]) ? mk[0] & ~atomicOr(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase), mk[0]) : 0u;
-                add_fresh_bits(fresh, a.sizes, P.sz_off + (int64_t)s * K * (nv + 1) + p, nv + 1, 0, lane);
+                if (mk[0] & ~cur[p]) atomicOr(mrow + (int64_t)p * P.nloc + (img[p] - P.vbase), mk[0]);
             }
         } else {
             for (int p = 0; p < nv; ++p) {
                 if (p == skip_p) continue;
                 uint32_t* rowm = a.M + P.m_off + (((int64_t)s * (nv + 1) + p) * P.nloc + (live ? img[p] - P.vbase : 0)) * mw;
-                const int64_t out = P.sz_off + (int64_t)s * K * (nv + 1) + p;
-                for (int w = 0; w < mw; ++w) add_fresh_bits(or_fresh(rowm + w, mk[w]), a.sizes, out, nv + 1, w, lane);
+                for (int w = 0; w < mw; ++w) or_bits(rowm + w, mk[w]);
             }
         }
     }
@@ -1422,17 +1401,9 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
             const unsigned peers = __match_any_sync(mask, key);
             if (lane == __ffs(peers) - 1) atomicAdd(a.counts + key, (unsigned long long)__popc(peers));
         }
-        if (mask) {
-            const int64_t out = P.sz_off + (int64_t)nsrc * K * (nv + 1);
-            for (int p = 0; p < nv; ++p) {
-                const uint32_t got =
-                    ok ? or_fresh(a.MB + P.b_off + ((int64_t)p * P.nloc + (img[p] - P.vbase)) * P.bw + (bk >> 5),
-                                  1u << (bk & 31))
-                       : 0u;
-                for (int w = 0; w < P.bw; ++w)
-                    add_fresh_bits((bk >> 5) == w ? got : 0u, a.sizes, out + p, nv, w, lane);
-            }
-        }
+        if (ok)
+            for (int p = 0; p < nv; ++p)
+                or_bits(a.MB + P.b_off + ((int64_t)p * P.nloc + (img[p] - P.vbase)) * P.bw + (bk >> 5), 1u << (bk & 31));
     }
 }
 
@@ -1619,6 +1590,48 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 
     acc.flush(a.counts, lane);
 }
 
+// Domain sizes from the mask planes: each set bit of a plane word adds one
+// vertex to its tuple's domain.  Block per (plane, run of 256 vertices) in
+// grid-stride loops; a warp transposes its 32 vertices' word w with one
+// ballot per bit set anywhere in the warp, and lane b holds bit b's count,
+// summed per block in shared memory and added once per block.
+__global__ void __launch_bounds__(256) k_mask_popcount(const MaskPlane* __restrict__ planes, int32_t nplanes,
+                                                     const uint32_t* __restrict__ M, const uint32_t* __restrict__ MB,
+                                                     uint32_t* __restrict__ sizes)
+{
+    __shared__ uint32_t hist[32 * kMaxMaskWords];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int32_t pl = blockIdx.y; pl < nplanes; pl += gridDim.y) {
+        const MaskPlane P = planes[pl];
+        const uint32_t* const base = (P.mb ? MB : M) + P.off;
+        const int W = P.words;
+        for (int i = threadIdx.x; i < 32 * W; i += blockDim.x) hist[i] = 0u;
+        __syncthreads();
+        for (int64_t v0 = (int64_t)blockIdx.x * blockDim.x + warp * 32; v0 < P.nloc;
+             v0 += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t v = v0 + lane;
+            for (int w = 0; w < W; ++w) {
+                const uint32_t word = v < P.nloc ? __ldcs(base + v * W + w) : 0u;
+                uint32_t any = __reduce_or_sync(kFull, word);
+                uint32_t mine = 0;
+                while (any) {
+                    const int b = __ffs(any) - 1;
+                    any &= any - 1;
+                    const uint32_t c = (uint32_t)__popc(__ballot_sync(kFull, (word >> b) & 1u));
+                    if (lane == b) mine = c;
+                }
+                if (mine) atomicAdd(hist + w * 32 + lane, mine);
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 32 * W; i += blockDim.x) {
+            const uint32_t c = hist[i];
+            if (c && i < P.nbits) atomicAdd(sizes + P.sz_base + (int64_t)i * P.sz_stride, c);
+        }
+        __syncthreads();
+    }
+}
+
 // Exclusive prefix of the touched-list lengths: the sweep's task numbering.
 __global__ void k_mask_prefix(int32_t nps, const uint32_t* __restrict__ tcount, unsigned long long* __restrict__ tprefix)
 {
@@ -1713,7 +1726,6 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
                                       : lower_bound_entry(a.adj, b, e, lo_key);
         uint32_t* Hs = a.H + P.h_off + (int64_t)s * P.mloc - P.ebase;
         uint32_t* NM = a.M + P.m_off + ((int64_t)s * (P.nv + 1) + P.nv) * P.nloc * mw;
-        const int64_t nm_out = P.sz_off + (int64_t)s * K * (P.nv + 1) + P.nv;
         unsigned long long* cnt = a.counts + P.key_base + (int64_t)s * K;
         if (use_acc && cnt != acc_cnt) {
             flush();
@@ -1755,13 +1767,7 @@ __global__ void __launch_bounds__(256) k_mask_sweep(MaskDev a)
                     atomicAdd(cnt + kc, v);
                 }
             }
-            const bool fresh = ok && diff > 0 && or_fresh(NM + (int64_t)(to - P.vbase) * mw + (kc >> 5), 1u << (kc & 31));
-            const unsigned fmask = __ballot_sync(kFull, fresh);
-            if (fresh) {
-                const unsigned peers = __match_any_sync(fmask, kc);
-                if (lane == __ffs(peers) - 1)
-                    atomicAdd(a.sizes + nm_out + (int64_t)kc * (P.nv + 1), (uint32_t)__popc(peers));
-            }
+            if (ok && diff > 0) or_bits(NM + (int64_t)(to - P.vbase) * mw + (kc >> 5), 1u << (kc & 31));
         }
         __syncwarp();
         if (use_acc) {
@@ -2112,6 +2118,17 @@ cudaError_t launch_clear(const ClearList& l, cudaStream_t st)
     const int64_t cap = (int64_t)sm_count() * 8;
     const int gx = (int)std::max<int64_t>(1, std::min(want, cap));
     k_clear<<<dim3(gx, l.n), 256, 0, st>>>(l);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mask_popcount(const MaskArgs& x, cudaStream_t st)
+{
+    if (x.nplanes == 0) return cudaSuccess;
+    const int gy = (int)std::min<int64_t>(x.nplanes, 65535);
+    const int64_t runs = (x.max_plane_nloc + 255) / 256;
+    const int64_t want = ((int64_t)sm_count() * 16 + gy - 1) / gy;
+    const int gx = (int)std::max<int64_t>(1, std::min(runs, want));
+    k_mask_popcount<<<dim3(gx, gy), 256, 0, st>>>(x.planes, x.nplanes, x.M, x.MB, x.sizes);
     return cudaGetLastError();
 }
 

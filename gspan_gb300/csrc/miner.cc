@@ -283,6 +283,41 @@ struct Run {
         return cudaMemcpyAsync(dst, src, bytes, kind, strm);
     }
 
+    // Device-to-host readbacks settled by one stream sync: the copies land in
+    // the context's pinned staging buffer and are then moved to their
+    // destinations (into pageable memory every copy would be a blocking round
+    // trip of its own).
+    struct Rb {
+        void* dst;
+        const void* src;
+        size_t bytes;
+    };
+    gspan_status readback(std::initializer_list<Rb> items, const char* what)
+    {
+        size_t need = 0;
+        for (const Rb& r : items) need += (r.bytes + 15) & ~(size_t)15;
+        if (need > ctx->h_stage_cap) {
+            if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+            ctx->h_stage = nullptr;
+            ctx->h_stage_cap = 0;
+            const size_t cap = std::max<size_t>(need + need / 2, (size_t)1 << 16);
+            GS_CK(cudaMallocHost(&ctx->h_stage, cap), "alloc readback staging");
+            ctx->h_stage_cap = cap;
+        }
+        size_t off = 0;
+        for (const Rb& r : items) {
+            if (r.bytes) GS_CK(copy(ctx->h_stage + off, r.src, r.bytes, cudaMemcpyDeviceToHost, s), what);
+            off += (r.bytes + 15) & ~(size_t)15;
+        }
+        GS_CK(wait(s), what);
+        off = 0;
+        for (const Rb& r : items) {
+            if (r.bytes) std::memcpy(r.dst, ctx->h_stage + off, r.bytes);
+            off += (r.bytes + 15) & ~(size_t)15;
+        }
+        return GSPAN_OK;
+    }
+
     bool use_hash(uint64_t count, int32_t nloc) const
     {
         const int mode = ctx->opts.domain_mode;
@@ -384,10 +419,9 @@ struct Run {
         if (profile) cudaEventRecord(ctx->ev_d, s);
         ++st.kernel_launches;
         std::vector<uint32_t> h((size_t)as.nact * kMaxV);
-        GS_CK(copy(h.data(), d_sizes, h.size() * 4, cudaMemcpyDeviceToHost, s), "read sizes");
         uint32_t status = 0;
-        GS_CK(copy(&status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
-        GS_CK(wait(s), "domain sizes");
+        gspan_status rc = readback({{h.data(), d_sizes, h.size() * 4}, {&status, ctx->d_status, 4}}, "domain sizes");
+        if (rc != GSPAN_OK) return rc;
         dfree(d_sizes, s);
         if (profile) {
             float ms = 0;
@@ -420,8 +454,10 @@ struct Run {
         ++st.kernel_launches;
         refresh_free();
         std::vector<unsigned long long> counts((size_t)nkeys);
-        GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read seed counts");
-        GS_CK(wait(s), "seed count");
+        {
+            const gspan_status rb = readback({{counts.data(), d_counts, (size_t)nkeys * 8}}, "seed count");
+            if (rb != GSPAN_OK) return rb;
+        }
         std::vector<Active> act;
         for (int64_t key = 0; key < nkeys; ++key) {
             const uint64_t c = counts[key];
@@ -680,7 +716,8 @@ struct Run {
         struct MGroup {
             std::vector<ParentMeta> metas;
             std::vector<int32_t> ps_parent;
-            int64_t tiles = 0, r = 0, h = 0, m = 0, b = 0, t = 0;
+            std::vector<MaskPlane> planes;   // mask planes counted after the sweep
+            int64_t tiles = 0, r = 0, h = 0, m = 0, b = 0, t = 0, max_nloc = 0;
             double bytes = 0;
         };
         std::vector<MGroup> groups;
@@ -743,6 +780,23 @@ struct Run {
             const int mvert = K <= kSweepAccKeys ? P.nv - 1 : P.nv;
             rows_bytes += (double)rows * (4.0 * P.nv + P.nsrc * (16.0 + 4.0 * g.segw + 4.0 * mvert * g.segw) +
                                           8.0 * P.nback);
+            // The parent's mask planes: per source, the old vertices' masks
+            // (ORed by the row pass; the source's own when the sweep does
+            // not count it) and the new vertex's (ORed by the sweep); per old
+            // vertex, the backward-tuple masks.
+            for (int s2 = 0; s2 < P.nsrc; ++s2)
+                for (int p = 0; p <= P.nv; ++p) {
+                    if (p == P.src_v[s2] && K <= kSweepAccKeys) continue;
+                    G.planes.push_back(MaskPlane{P.m_off + ((int64_t)s2 * (P.nv + 1) + p) * P.nloc * g.segw,
+                                                 P.sz_off + (int64_t)s2 * K * (P.nv + 1) + p, P.nloc, P.nv + 1, K,
+                                                 (int16_t)g.segw, 0});
+                }
+            if (P.nback > 0)
+                for (int p = 0; p < P.nv; ++p)
+                    G.planes.push_back(MaskPlane{P.b_off + (int64_t)p * P.nloc * P.bw,
+                                                 P.sz_off + (int64_t)P.nsrc * K * (P.nv + 1) + p, P.nloc, P.nv,
+                                                 P.nback * g.nel, (int16_t)P.bw, 1});
+            G.max_nloc = std::max<int64_t>(G.max_nloc, P.nloc);
             G.metas.push_back(P);
         }
         size_t nmask = 0;
@@ -756,6 +810,7 @@ struct Run {
         uint32_t* d_tcount = nullptr;
         int32_t *d_touched = nullptr, *d_psp = nullptr;
         unsigned long long* d_tprefix = nullptr;
+        MaskPlane* d_planes = nullptr;
         auto release = [&]() {
             dfree(d_up, s);
             dfree(d_counts, s);
@@ -771,6 +826,7 @@ struct Run {
             dfree(d_touched, s);
             dfree(d_psp, s);
             dfree(d_tprefix, s);
+            dfree(d_planes, s);
         };
         struct Guard {
             std::function<void()> f;
@@ -793,8 +849,9 @@ struct Run {
             for (uint64_t r : gen->rows) st.fused_rows += r;
         }
         if (!groups.empty()) {
-            int64_t mr = 0, mh = 0, mm = 0, mb = 0, mt = 0, mps = 0, mmeta = 0;
+            int64_t mr = 0, mh = 0, mm = 0, mb = 0, mt = 0, mps = 0, mmeta = 0, mpl = 0;
             for (const MGroup& G : groups) {
+                mpl = std::max<int64_t>(mpl, (int64_t)G.planes.size());
                 mr = std::max(mr, G.r);
                 mh = std::max(mh, G.h);
                 mm = std::max(mm, G.m);
@@ -812,6 +869,7 @@ struct Run {
             GS_CK(dalloc(&d_tprefix, (size_t)mps + 1, s), "alloc touched prefix");
             GS_CK(dalloc(&d_psp, (size_t)mps, s), "alloc slot parents");
             GS_CK(dalloc(&d_mg, (size_t)mmeta, s), "alloc mask parents");
+            GS_CK(dalloc(&d_planes, (size_t)std::max<int64_t>(mpl, 1), s), "alloc mask planes");
             GS_CK(dalloc(&d_sizes, (size_t)std::max<int64_t>(sz_total, 1), s), "alloc sizes");
             clr.add(d_R, mr);
             clr.add(d_H, std::max<int64_t>(mh, 1));
@@ -822,6 +880,9 @@ struct Run {
                       "copy mask parents");
                 GS_CK(copy(d_psp, G.ps_parent.data(), G.ps_parent.size() * 4, cudaMemcpyHostToDevice, s),
                       "copy slot parents");
+                if (!G.planes.empty())
+                    GS_CK(copy(d_planes, G.planes.data(), G.planes.size() * sizeof(MaskPlane), cudaMemcpyHostToDevice, s),
+                          "copy mask planes");
                 // Per group: its masks, touched counts and tile counter (the
                 // sweep leaves R and H zero); the first group's go with the
                 // level's clears.
@@ -869,7 +930,13 @@ struct Run {
                 tic(&e0, &e1);
                 GS_CK(launch_mask_sweep(ma, s), "mask sweep launch");
                 toc(e0, e1, &st.sweep_ms);
-                st.kernel_launches += 3;
+                ma.planes = d_planes;
+                ma.nplanes = (int32_t)G.planes.size();
+                ma.max_plane_nloc = G.max_nloc;
+                tic(&e0, &e1);
+                GS_CK(launch_mask_popcount(ma, s), "mask popcount launch");
+                toc(e0, e1, &st.domain_ms);
+                st.kernel_launches += 4;
                 st.rows_launches += 1;
             }
             st.rows_bytes += rows_bytes;
@@ -921,11 +988,14 @@ struct Run {
         std::vector<uint32_t> sizes((size_t)sz_total);
         unsigned long long ctr[4] = {0, 0, 0, 0};
         uint32_t mstat = 0;
-        GS_CK(copy(counts.data(), d_counts, nkeys * 8, cudaMemcpyDeviceToHost, s), "read counts");
-        if (sz_total) GS_CK(copy(sizes.data(), d_sizes, sz_total * 4, cudaMemcpyDeviceToHost, s), "read sizes");
-        GS_CK(copy(ctr, ctx->d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s), "read counters");
-        GS_CK(copy(&mstat, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read status");
-        GS_CK(wait(s), "extension count");
+        {
+            const gspan_status rb = readback({{counts.data(), d_counts, (size_t)nkeys * 8},
+                                              {sizes.data(), d_sizes, (size_t)sz_total * 4},
+                                              {ctr, ctx->d_counters, sizeof(ctr)},
+                                              {&mstat, ctx->d_status, 4}},
+                                             "extension count");
+            if (rb != GSPAN_OK) return rb;
+        }
         resolve();
         settle();
         st.scanned_entries += ctr[1] + ctr[3];

@@ -41,6 +41,9 @@ struct gspan_ctx {
     // Pinned host words for readbacks that are settled at a later sync.
     unsigned long long* h_pin = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_c = nullptr, ev_d = nullptr;
+    // Pinned staging for the miner's device-to-host readbacks (grown on demand).
+    uint8_t* h_stage = nullptr;
+    size_t h_stage_cap = 0;
     // Event pairs for kernel timing (profile mode), kept across runs.
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
     int live_graphs = 0;
