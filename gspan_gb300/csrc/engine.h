@@ -90,6 +90,11 @@ struct DevGraph {
     // the adjacency.  Not built (null) above 2^30 entries.
     uint64_t* eidx = nullptr;
     uint32_t eidx_cap = 0;
+    // Embeddings per 1-edge tuple (nvl * nel * lwin keys), counted once at
+    // upload: device and host copies, null / empty when the key space is
+    // larger than kSeedCacheKeys (mining counts them per run then).
+    unsigned long long* seed_counts = nullptr;
+    std::vector<unsigned long long> seed_counts_h;
     // Some vertex has two equal entries (parallel edges with one label).
     bool parallel = true;
     // Some vertex has an entry to itself.  Without self-loops every embedding
@@ -113,6 +118,8 @@ constexpr int kSweepAccKeys = 64;
 
 // Widest per-vertex key mask the mask kernels handle (x 32 keys).
 constexpr int kMaxMaskWords = 16;
+// Largest 1-edge key space whose seed counts the store keeps.
+constexpr int64_t kSeedCacheKeys = (int64_t)1 << 22;
 // Mask words of the row pass's fast build (<= 128 tuple keys per label
 // window); wider label spaces use the kMaxMaskWords build.
 constexpr int kNarrowMaskWords = 4;
@@ -199,6 +206,8 @@ struct ParentMeta {
     int16_t gen_kind;
     int16_t gen_s;
     int32_t gen_kc;
+    // 2^32 rows or more: the row pass checks its 32-bit counters for a wrap.
+    int32_t r_wide;
 };
 
 // Per-level key space arrays on the device.

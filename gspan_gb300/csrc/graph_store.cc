@@ -79,6 +79,9 @@ void free_graph(gspan_graph* gr, cudaStream_t st)
     g.eidx_cap = 0;
     if (g.win_base) cudaFreeAsync(g.win_base, st);
     g.win_base = nullptr;
+    if (g.seed_counts) cudaFreeAsync(g.seed_counts, st);
+    g.seed_counts = nullptr;
+    g.seed_counts_h.clear();
     g.segmask = nullptr;
     g.selfloop = nullptr;
     g.offsets = nullptr;
@@ -375,6 +378,19 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
         UP_CK(cudaMemsetAsync(g.eidx, 0xFF, (size_t)cap * 8, s), "clear edge index");
     }
     UP_CK(launch_entry_flags(g, ctx->d_status, s), "entry flags launch");
+    // Seed counts: a property of the graph alone, counted once here and read
+    // with the flags, so mining runs start from them.
+    {
+        const int64_t nkeys = (int64_t)g.nvl * g.nel * g.lwin;
+        if (M > 0 && nkeys > 0 && nkeys <= kSeedCacheKeys) {
+            UP_CK(cudaMallocAsync(&g.seed_counts, (size_t)nkeys * 8, s), "alloc seed counts");
+            UP_CK(cudaMemsetAsync(g.seed_counts, 0, (size_t)nkeys * 8, s), "clear seed counts");
+            UP_CK(launch_seed_count(g, g.seed_counts, s), "seed count launch");
+            g.seed_counts_h.resize((size_t)nkeys);
+            UP_CK(cudaMemcpyAsync(g.seed_counts_h.data(), g.seed_counts, (size_t)nkeys * 8, cudaMemcpyDeviceToHost, s),
+                  "read seed counts");
+        }
+    }
     {
         uint32_t flags = 0;
         UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");

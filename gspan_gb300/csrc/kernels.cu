@@ -1124,30 +1124,21 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
     for (int s = 0; s < nsrc; ++s) {
         const int32_t u = live ? img[P.src_v[s]] : -1;
         const unsigned lm = __ballot_sync(kFull, live);
-        bool first_row = false;   // this lane's group made R[u] non-zero
         if (live) {
+            // One add per group of lanes with the same source image; the
+            // touched lists are built from R afterwards (k_mask_touched), so
+            // the old value is not waited for - except for a parent with
+            // 2^32 rows or more, where a 32-bit counter (R, and H <= R) could
+            // wrap: that fails the job.
             const unsigned peers = __match_any_sync(lm, u);
             if (lane == __ffs(peers) - 1) {
+                uint32_t* const Ru = a.R + P.r_off + (int64_t)s * P.nloc + (u - P.vbase);
                 const uint32_t add = (uint32_t)__popc(peers);
-                const uint32_t before = atomicAdd(a.R + P.r_off + (int64_t)s * P.nloc + (u - P.vbase), add);
-                first_row = before == 0;
-                // R (and H <= R) are 32-bit: a wrap would corrupt counts, so it fails the job.
-                if (before > 0xFFFFFFFFu - add) atomicOr(a.status, kErrCounter);
-            }
-        }
-        // One append per warp for the source images seen for the first time.
-        const unsigned fm = __ballot_sync(kFull, first_row);
-        if (fm) {
-            const int first = __ffs(fm) - 1;
-            uint32_t base = 0;
-            if (lane == first) base = atomicAdd(a.tcount + P.ps_begin + s, (uint32_t)__popc(fm));
-            base = __shfl_sync(kFull, base, first);
-            if (first_row) {
-                const uint32_t slot = base + __popc(fm & lanemask_lt());
-                if (slot < (uint32_t)P.t_cap)
-                    a.touched[P.t_off + (int64_t)s * P.t_cap + slot] = u;
-                else
-                    atomicOr(a.status, kErrCursor);
+                if (P.r_wide) {
+                    if (atomicAdd(Ru, add) > 0xFFFFFFFFu - add) atomicOr(a.status, kErrCounter);
+                } else {
+                    atomicAdd(Ru, add);
+                }
             }
         }
         uint32_t mk[MW] = {};
@@ -1629,6 +1620,48 @@ __global__ void __launch_bounds__(256) k_mask_popcount(const MaskPlane* __restri
             if (c && i < P.nbits) atomicAdd(sizes + P.sz_base + (int64_t)i * P.sz_stride, c);
         }
         __syncthreads();
+    }
+}
+
+// Touched lists from R: every vertex of a (parent, source) slot's window
+// whose row counter is non-zero, in vertex order.  Block rows (blockIdx.y)
+// walk the slots, blocks along x the window in runs of 256 vertices, with one
+// reservation in the slot's count per run.
+__global__ void __launch_bounds__(256) k_mask_touched(MaskDev a)
+{
+    __shared__ uint32_t wcnt[8];
+    __shared__ uint32_t run_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int32_t q = blockIdx.y; q < a.nps; q += gridDim.y) {
+        const ParentMeta& P = a.parents[a.ps_parent[q]];
+        const int s = q - P.ps_begin;
+        const uint32_t* const Rs = a.R + P.r_off + (int64_t)s * P.nloc;
+        int32_t* const out = a.touched + P.t_off + (int64_t)s * P.t_cap;
+        for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < P.nloc; b0 += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t v = b0 + threadIdx.x;
+            const bool hit = v < P.nloc && __ldcg(Rs + v) != 0u;
+            const unsigned hm = __ballot_sync(kFull, hit);
+            if (lane == 0) wcnt[warp] = (uint32_t)__popc(hm);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t run = 0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                    const uint32_t c = wcnt[w];
+                    wcnt[w] = run;
+                    run += c;
+                }
+                run_base = run ? atomicAdd(a.tcount + q, run) : 0u;
+            }
+            __syncthreads();
+            if (hit) {
+                const uint32_t slot = run_base + wcnt[warp] + (uint32_t)__popc(hm & lanemask_lt());
+                if (slot < (uint32_t)P.t_cap)
+                    out[slot] = (int32_t)(P.vbase + v);
+                else
+                    atomicOr(a.status, kErrCursor);
+            }
+            __syncthreads();
+        }
     }
 }
 
@@ -2135,6 +2168,13 @@ cudaError_t launch_mask_popcount(const MaskArgs& x, cudaStream_t st)
 cudaError_t launch_mask_sweep(const MaskArgs& x, cudaStream_t st)
 {
     if (x.nps == 0) return cudaSuccess;
+    {
+        const int gy = (int)std::min<int64_t>(x.nps, 65535);
+        const int64_t runs = (x.max_plane_nloc + 255) / 256;
+        const int64_t want = ((int64_t)sm_count() * 16 + gy - 1) / gy;
+        const int gx = (int)std::max<int64_t>(1, std::min(runs, want));
+        k_mask_touched<<<dim3(gx, gy), 256, 0, st>>>(mask_dev(x));
+    }
     k_mask_prefix<<<1, 32, 0, st>>>(x.nps, x.tcount, x.tprefix);
     k_mask_sweep<<<sm_count() * 8, 256, 0, st>>>(mask_dev(x));
     return cudaGetLastError();

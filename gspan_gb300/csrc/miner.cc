@@ -446,18 +446,24 @@ struct Run {
         if (nkeys > (int64_t)std::numeric_limits<int32_t>::max())
             return fail(ctx, GSPAN_ERR_LIMIT, "too many distinct labels for the 1-edge key space");
         if (g.m == 0 || nkeys == 0) return GSPAN_OK;
-        unsigned long long* d_counts = nullptr;
-        GS_CK(dalloc(&d_counts, (size_t)nkeys, s), "alloc seed counts");
-        GS_CK(cudaMemsetAsync(d_counts, 0, nkeys * 8, s), "clear seed counts");
+        // The counts per 1-edge tuple depend on the graph alone: the store
+        // keeps them (device and host copies) when its key space is small
+        // enough, else they are counted here.
+        const bool cached = g.seed_counts != nullptr;
+        unsigned long long* d_counts = g.seed_counts;
+        std::vector<unsigned long long> counted;
         if (profile) cudaEventRecord(ctx->ev_a, s);
-        GS_CK(launch_seed_count(g, d_counts, s), "seed count launch");
-        ++st.kernel_launches;
-        refresh_free();
-        std::vector<unsigned long long> counts((size_t)nkeys);
-        {
-            const gspan_status rb = readback({{counts.data(), d_counts, (size_t)nkeys * 8}}, "seed count");
+        if (!cached) {
+            GS_CK(dalloc(&d_counts, (size_t)nkeys, s), "alloc seed counts");
+            GS_CK(cudaMemsetAsync(d_counts, 0, nkeys * 8, s), "clear seed counts");
+            GS_CK(launch_seed_count(g, d_counts, s), "seed count launch");
+            ++st.kernel_launches;
+            refresh_free();
+            counted.resize((size_t)nkeys);
+            const gspan_status rb = readback({{counted.data(), d_counts, (size_t)nkeys * 8}}, "seed count");
             if (rb != GSPAN_OK) return rb;
         }
+        const unsigned long long* const counts = cached ? g.seed_counts_h.data() : counted.data();
         std::vector<Active> act;
         for (int64_t key = 0; key < nkeys; ++key) {
             const uint64_t c = counts[key];
@@ -481,6 +487,7 @@ struct Run {
                   "seed support launch");
             ++st.kernel_launches;
         }
+        if (cached) refresh_free();
         if (profile) cudaEventRecord(ctx->ev_b, s);
         std::vector<int> sup;
         rc = supports(as, sup);
@@ -496,7 +503,7 @@ struct Run {
             if (k > 1) next.push_back(Parent{act[a].code, as.mat[a], as.mat[a] + (int64_t)act[a].count});
         }
         as.release(s);
-        dfree(d_counts, s);
+        if (!cached) dfree(d_counts, s);
         return GSPAN_OK;
     }
 
@@ -676,6 +683,7 @@ struct Run {
                 P.gen_s = gen->s[i];
                 P.gen_kc = gen->kc[i];
             }
+            P.r_wide = P.row_end - P.row_begin >= ((int64_t)1 << 32) ? 1 : 0;
             P.key_base = (int32_t)nkeys;
             key_span[i] = (int64_t)P.nsrc * K + (int64_t)P.nback * g.nel;
             nkeys += key_span[i];
@@ -914,6 +922,7 @@ struct Run {
                 ma.tile_counter = ctx->d_counters + 2;
                 ma.scanned = ctx->d_counters + 3;
                 ma.status = ctx->d_status;
+                ma.max_plane_nloc = G.max_nloc;
                 tic(&e0, &e1);
                 if (gen) {
                     ma.in_col_ptrs = nullptr;
@@ -932,7 +941,6 @@ struct Run {
                 toc(e0, e1, &st.sweep_ms);
                 ma.planes = d_planes;
                 ma.nplanes = (int32_t)G.planes.size();
-                ma.max_plane_nloc = G.max_nloc;
                 tic(&e0, &e1);
                 GS_CK(launch_mask_popcount(ma, s), "mask popcount launch");
                 toc(e0, e1, &st.domain_ms);
