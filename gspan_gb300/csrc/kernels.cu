@@ -1581,11 +1581,28 @@ __global__ void __launch_bounds__(kMaskWarps * 32, MW <= kNarrowMaskWords ? 5 : 
     acc.flush(a.counts, lane);
 }
 
+// Transposes the warp's 32x32 bit matrix (lane i's word is row i): afterwards
+// lane b holds column b, bit i of it being bit b of lane i's word.  Five
+// exchange steps, each swapping the off-diagonal blocks of the next smaller
+// block size (the recursive block transpose, done across lanes).
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane)
+{
+    const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const int j = 16 >> k;
+        const uint32_t m = masks[k];
+        const uint32_t y = __shfl_xor_sync(kFull, x, j);
+        x = (lane & j) ? (x & ~m) | ((y & ~m) >> j) : (x & m) | ((y & m) << j);
+    }
+    return x;
+}
+
 // Domain sizes from the mask planes: each set bit of a plane word adds one
 // vertex to its tuple's domain.  Block per (plane, run of 256 vertices) in
-// grid-stride loops; a warp transposes its 32 vertices' word w with one
-// ballot per bit set anywhere in the warp, and lane b holds bit b's count,
-// summed per block in shared memory and added once per block.
+// grid-stride loops; a warp transposes its 32 vertices' word w, so lane b
+// counts bit b with one popcount, summed per block in shared memory and
+// added once per block.
 __global__ void __launch_bounds__(256) k_mask_popcount(const MaskPlane* __restrict__ planes, int32_t nplanes,
                                                      const uint32_t* __restrict__ M, const uint32_t* __restrict__ MB,
                                                      uint32_t* __restrict__ sizes)
@@ -1603,15 +1620,9 @@ __global__ void __launch_bounds__(256) k_mask_popcount(const MaskPlane* __restri
             const int64_t v = v0 + lane;
             for (int w = 0; w < W; ++w) {
                 const uint32_t word = v < P.nloc ? __ldcs(base + v * W + w) : 0u;
-                uint32_t any = __reduce_or_sync(kFull, word);
-                uint32_t mine = 0;
-                while (any) {
-                    const int b = __ffs(any) - 1;
-                    any &= any - 1;
-                    const uint32_t c = (uint32_t)__popc(__ballot_sync(kFull, (word >> b) & 1u));
-                    if (lane == b) mine = c;
-                }
-                if (mine) atomicAdd(hist + w * 32 + lane, mine);
+                if (!__any_sync(kFull, word)) continue;
+                const uint32_t c = (uint32_t)__popc(warp_transpose32(word, lane));
+                if (c) atomicAdd(hist + w * 32 + lane, c);
             }
         }
         __syncthreads();
