@@ -549,18 +549,28 @@ struct ExpandDev {
 // [32][ss] (per row and range: first adjacency entry, entries), pre [32]
 // (exclusive prefix of the rows' entry counts).  vs, ss are odd (no bank
 // conflicts between lanes).
-// Materialize also keeps a per-slot 64-bit cursor [ss] (2 * ss ints) after them.
-__host__ __device__ inline int expand_warp_ints(int vs, int ss) { return 32 * (vs + 2 * ss + 1) + 2 * ss; }
+// Materialize also keeps a per-slot 64-bit cursor [ss] (2 * ss ints) after
+// them, then per slot a 64-bit row limit [ss] and an active index (2 * ss
+// ints), and the records of up to kMatChunk candidates [3][kMatChunk].
+constexpr int kMatChunk = 256;
+__host__ __device__ inline int expand_warp_ints(int vs, int ss, bool mat)
+{
+    return 32 * (vs + 2 * ss + 1) + 2 * ss + (mat ? 4 * ss + 3 * kMatChunk : 0);
+}
 
 template <Pass kPass>
 __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    int32_t* const Wimg = reinterpret_cast<int32_t*>(smem_raw) + (threadIdx.x >> 5) * expand_warp_ints(a.vs, a.ss);
+    int32_t* const Wimg = reinterpret_cast<int32_t*>(smem_raw) +
+                          (threadIdx.x >> 5) * expand_warp_ints(a.vs, a.ss, kPass == Pass::Materialize);
     int32_t* const Wstart = Wimg + 32 * a.vs;
     int32_t* const Wcnt = Wstart + 32 * a.ss;
     int32_t* const Wpre = Wcnt + 32 * a.ss;
     unsigned long long* const Wcur = reinterpret_cast<unsigned long long*>(Wpre + 32);
+    unsigned long long* const Wlim = Wcur + a.ss;                       // Materialize only
+    int32_t* const Wai = reinterpret_cast<int32_t*>(Wlim + a.ss);      // Materialize only
+    int32_t* const Wrec = Wai + 2 * a.ss;                                // Materialize only
     const int lane = threadIdx.x & 31;
     const int32_t LeLv = a.nel * a.lwin;
 
@@ -738,57 +748,79 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
                 for (int p = 0; p < nv; ++p) fresh &= Wimg[l2 * a.vs + p] != (int32_t)*to;
                 return fresh;
             };
-            if (lane < nslot) Wcur[lane] = 0;
-            __syncwarp();
-            for (int32_t base = 0; base < total; base += 32) {
-                int owner = 0, q = 0;
-                int32_t ei = 0;
-                uint32_t to = 0;
-                const bool ok = base + lane < total && candidate(base + lane, &owner, &q, &ei, &to);
-                const unsigned m = __ballot_sync(kFull, ok);
-                if (ok) {
-                    const unsigned peers = __match_any_sync(m, q);
-                    if (lane == __ffs(peers) - 1) atomicAdd(Wcur + q, (unsigned long long)__popc(peers));
-                }
-            }
-            __syncwarp();
-            if (lane < nslot) {
-                const int32_t key = key_base + P.mseg_s[lane] * LeLv + (int32_t)P.mseg_kc[lane];
-                const int32_t ai = a.keys.act[key];
-                const unsigned long long n = Wcur[lane];
-                Wcur[lane] = (n && ai >= 0) ? atomicAdd(a.keys.cursor + ai, n) : 0ull;
-            }
-            __syncwarp();
-            for (int32_t base = 0; base < total; base += 32) {
-                int owner = 0, q = 0;
-                int32_t ei = 0;
-                uint32_t to = 0;
-                const bool ok = base + lane < total && candidate(base + lane, &owner, &q, &ei, &to);
-                const int32_t key = key_base + P.mseg_s[q] * LeLv + (int32_t)P.mseg_kc[q];
-                const int32_t ai = ok ? a.keys.act[key] : -1;
-                const bool mat = ai >= 0;
-                const unsigned mm = __ballot_sync(kFull, mat);
-                if (mat) {
-                    const unsigned peers = __match_any_sync(mm, q);
-                    const int leader = __ffs(peers) - 1;
-                    unsigned long long at = 0;
-                    if (lane == leader) at = atomicAdd(Wcur + q, (unsigned long long)__popc(peers));
-                    at = __shfl_sync(mm, at, leader);
-                    const unsigned long long slot = at + __popc(peers & lanemask_lt());
-                    if (slot < a.keys.counts[key]) {
-                        const long long r = a.keys.mat_off[ai] + (long long)slot;
-                        for (int p = 0; p < nv; ++p) a.out_cols[p][r] = Wimg[owner * a.vs + p];
-                        a.out_cols[nv][r] = (int32_t)to;
-                        if (a.ecol_out >= 0) {
-                            const int64_t orow = P.row_begin + (tile - P.tile_begin) * kRows + owner;
-                            for (int jj = 0; jj < P.nedge; ++jj)
-                                a.out_cols[a.ecol_out + jj][r] = __ldg(a.in_cols[a.ecol_in + jj] + orow);
-                            a.out_cols[a.ecol_out + P.nedge][r] = ei;
-                        }
-                    } else {
-                        atomicOr(a.status, kErrCursor);
+            // Candidates go in chunks of kMatChunk: the counting pass keeps
+            // each one's `to` (-1: not a child), entry and (owner, slot) in
+            // shared memory, so the writing pass reads them back instead of
+            // searching for them again.
+            int32_t* const Rto = Wrec;
+            int32_t* const Rei = Wrec + kMatChunk;
+            int32_t* const Roq = Wrec + 2 * kMatChunk;
+            for (int32_t cb = 0; cb < total; cb += kMatChunk) {
+                const int32_t cn = min(kMatChunk, total - cb);
+                if (lane < nslot) Wcur[lane] = 0;
+                __syncwarp();
+                for (int32_t base = 0; base < cn; base += 32) {
+                    const int32_t item = base + lane;
+                    int owner = 0, q = 0;
+                    int32_t ei = 0;
+                    uint32_t to = 0;
+                    const bool ok = item < cn && candidate(cb + item, &owner, &q, &ei, &to);
+                    if (item < cn) {
+                        Rto[item] = ok ? (int32_t)to : -1;
+                        Rei[item] = ei;
+                        Roq[item] = (owner << 8) | q;
+                    }
+                    const unsigned m = __ballot_sync(kFull, ok);
+                    if (ok) {
+                        const unsigned peers = __match_any_sync(m, q);
+                        if (lane == __ffs(peers) - 1) atomicAdd(Wcur + q, (unsigned long long)__popc(peers));
                     }
                 }
+                __syncwarp();
+                if (lane < nslot) {
+                    const int32_t key = key_base + P.mseg_s[lane] * LeLv + (int32_t)P.mseg_kc[lane];
+                    const int32_t ai = a.keys.act[key];
+                    const unsigned long long n = Wcur[lane];
+                    Wcur[lane] = (n && ai >= 0) ? atomicAdd(a.keys.cursor + ai, n) : 0ull;
+                    Wai[lane] = ai;
+                    Wlim[lane] = a.keys.counts[key];
+                }
+                __syncwarp();
+                for (int32_t base = 0; base < cn; base += 32) {
+                    const int32_t item = base + lane;
+                    int32_t to = -1, ei = 0, oq = 0;
+                    if (item < cn) {
+                        to = Rto[item];
+                        ei = Rei[item];
+                        oq = Roq[item];
+                    }
+                    const int q = oq & 0xFF, owner = oq >> 8;
+                    const int32_t ai = to >= 0 ? Wai[q] : -1;
+                    const bool mat = ai >= 0;
+                    const unsigned mm = __ballot_sync(kFull, mat);
+                    if (mat) {
+                        const unsigned peers = __match_any_sync(mm, q);
+                        const int leader = __ffs(peers) - 1;
+                        unsigned long long at = 0;
+                        if (lane == leader) at = atomicAdd(Wcur + q, (unsigned long long)__popc(peers));
+                        at = __shfl_sync(mm, at, leader);
+                        const unsigned long long slot = at + __popc(peers & lanemask_lt());
+                        if (slot < Wlim[q]) {
+                            const long long r = a.keys.mat_off[ai] + (long long)slot;
+                            for (int p = 0; p < nv; ++p) a.out_cols[p][r] = Wimg[owner * a.vs + p];
+                            a.out_cols[nv][r] = to;
+                            if (a.ecol_out >= 0) {
+                                const int64_t orow = P.row_begin + (tile - P.tile_begin) * kRows + owner;
+                                for (int jj = 0; jj < P.nedge; ++jj)
+                                    a.out_cols[a.ecol_out + jj][r] = __ldg(a.in_cols[a.ecol_in + jj] + orow);
+                                a.out_cols[a.ecol_out + P.nedge][r] = ei;
+                            }
+                        } else {
+                            atomicOr(a.status, kErrCursor);
+                        }
+                    }
+                }
+                __syncwarp();
             }
             __syncwarp();
             continue;
@@ -1950,10 +1982,11 @@ int expand_grid_blocks(int device)
     // Allow the largest scratch (kMaxV vertices and ranges) on this device.
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const size_t smem = (size_t)kExpandWarps * 4 * expand_warp_ints(kMaxV | 1, kMaxV | 1);
+    const size_t smem = (size_t)kExpandWarps * 4 * expand_warp_ints(kMaxV | 1, kMaxV | 1, false);
+    const size_t smem_mat = (size_t)kExpandWarps * 4 * expand_warp_ints(kMaxV | 1, kMaxV | 1, true);
     cudaFuncSetAttribute(k_expand<Pass::Count>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_expand<Pass::Support>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_expand<Pass::Materialize>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_expand<Pass::Materialize>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_mat);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_expand<Pass::Support>, kExpandThreads, smem);
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm;
@@ -1992,7 +2025,7 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
     }
     a.vs = maxv | 1;
     a.ss = maxs | 1;
-    const size_t smem = (size_t)kExpandWarps * 4 * expand_warp_ints(a.vs, a.ss);
+    const size_t smem = (size_t)kExpandWarps * 4 * expand_warp_ints(a.vs, a.ss, pass == Pass::Materialize);
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
