@@ -6,6 +6,7 @@
 #include "miner.h"
 
 #include <algorithm>
+#include <cstring>
 #include <climits>
 #include <new>
 
@@ -349,52 +350,72 @@ gspan_status upload_graphs(gspan_ctx* ctx, int32_t ninst, const int32_t* ns, con
     // per-vertex segment masks and starts (for the mask extension path, when
     // the window's tuple space fits the mask width), self-loop bits and the
     // symmetry check, and the edge index (load factor in (3/8, 3/4]).
-    UP_CK(cudaMemsetAsync(ctx->d_status, 0, 4, s), "clear status");
+    // Everything these passes need zeroed (or, for the edge index, ~0) is
+    // allocated first and cleared by one launch.
+    ClearList clr;
+    clr.add(ctx->d_status, 1);
     {
         const int64_t K = (int64_t)g.nel * g.lwin;
         if (N > 0 && K > 0 && K <= 32 * kMaxMaskWords) {
             g.segw = (int32_t)((K + 31) / 32);
             UP_CK(cudaMallocAsync(&g.segmask, (size_t)N * g.segw * 4, s), "alloc segment masks");
             UP_CK(cudaMallocAsync(&g.segone, (size_t)N * g.segw * 4, s), "alloc segment masks");
-            UP_CK(cudaMemsetAsync(g.segmask, 0, (size_t)N * g.segw * 4, s), "clear segment masks");
-            UP_CK(cudaMemsetAsync(g.segone, 0, (size_t)N * g.segw * 4, s), "clear segment masks");
+            clr.add(g.segmask, (int64_t)N * g.segw);
+            clr.add(g.segone, (int64_t)N * g.segw);
             const int64_t k1 = K + 1;
             if ((double)N * k1 * 4 <= 4.0 * (1u << 30))
                 UP_CK(cudaMallocAsync(&g.segstart, (size_t)N * k1 * 4, s), "alloc segment starts");
-            UP_CK(launch_segments(g, s), "segment launch");
         }
     }
     {
         const size_t words = ((size_t)N + 31) / 32 + 1;
         UP_CK(cudaMallocAsync(&g.selfloop, words * 4, s), "alloc self-loop bits");
         if (M > 0) UP_CK(cudaMallocAsync(&g.rev, (size_t)M * 4, s), "alloc reverse entries");
-        UP_CK(cudaMemsetAsync(g.selfloop, 0, words * 4, s), "clear self-loop bits");
+        clr.add(g.selfloop, (int64_t)words);
     }
     if (M > 0 && M <= (1 << 30)) {
         uint32_t cap = 64;
         while ((uint64_t)cap < (uint64_t)M + M / 3) cap <<= 1;
         UP_CK(cudaMallocAsync(&g.eidx, (size_t)cap * 8, s), "alloc edge index");
         g.eidx_cap = cap;
-        UP_CK(cudaMemsetAsync(g.eidx, 0xFF, (size_t)cap * 8, s), "clear edge index");
+        clr.add(g.eidx, (int64_t)cap * 2, 0xFFFFFFFFu);
     }
-    UP_CK(launch_entry_flags(g, ctx->d_status, s), "entry flags launch");
     // Seed counts: a property of the graph alone, counted once here and read
     // with the flags, so mining runs start from them.
-    {
-        const int64_t nkeys = (int64_t)g.nvl * g.nel * g.lwin;
-        if (M > 0 && nkeys > 0 && nkeys <= kSeedCacheKeys) {
-            UP_CK(cudaMallocAsync(&g.seed_counts, (size_t)nkeys * 8, s), "alloc seed counts");
-            UP_CK(cudaMemsetAsync(g.seed_counts, 0, (size_t)nkeys * 8, s), "clear seed counts");
-            UP_CK(launch_seed_count(g, g.seed_counts, s), "seed count launch");
-            g.seed_counts_h.resize((size_t)nkeys);
-            UP_CK(cudaMemcpyAsync(g.seed_counts_h.data(), g.seed_counts, (size_t)nkeys * 8, cudaMemcpyDeviceToHost, s),
-                  "read seed counts");
-        }
+    const int64_t seed_keys = (int64_t)g.nvl * g.nel * g.lwin;
+    const bool keep_seeds = M > 0 && seed_keys > 0 && seed_keys <= kSeedCacheKeys;
+    if (keep_seeds) {
+        UP_CK(cudaMallocAsync(&g.seed_counts, (size_t)seed_keys * 8, s), "alloc seed counts");
+        clr.add(g.seed_counts, seed_keys * 2);
     }
+    UP_CK(launch_clear(clr, s), "clear launch");
+    if (g.segw > 0) UP_CK(launch_segments(g, s), "segment launch");
+    UP_CK(launch_entry_flags(g, ctx->d_status, s), "entry flags launch");
+    if (keep_seeds) UP_CK(launch_seed_count(g, g.seed_counts, s), "seed count launch");
     {
-        uint32_t flags = 0;
-        UP_CK(cudaMemcpyAsync(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
+        // Flags and seed counts come back through the context's pinned
+        // staging, settled by one sync.
+        const size_t seed_bytes = keep_seeds ? (size_t)seed_keys * 8 : 0;
+        const size_t need = 16 + seed_bytes;
+        if (need > ctx->h_stage_cap) {
+            if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+            ctx->h_stage = nullptr;
+            ctx->h_stage_cap = 0;
+            const size_t cap = std::max<size_t>(need + need / 2, (size_t)1 << 16);
+            UP_CK(cudaMallocHost(&ctx->h_stage, cap), "alloc readback staging");
+            ctx->h_stage_cap = cap;
+        }
+        UP_CK(cudaMemcpyAsync(ctx->h_stage, ctx->d_status, 4, cudaMemcpyDeviceToHost, s), "read flags");
+        if (keep_seeds)
+            UP_CK(cudaMemcpyAsync(ctx->h_stage + 16, g.seed_counts, seed_bytes, cudaMemcpyDeviceToHost, s),
+                  "read seed counts");
         UP_CK(cudaStreamSynchronize(s), "graph flags");
+        uint32_t flags = 0;
+        std::memcpy(&flags, ctx->h_stage, 4);
+        if (keep_seeds) {
+            g.seed_counts_h.resize((size_t)seed_keys);
+            std::memcpy(g.seed_counts_h.data(), ctx->h_stage + 16, seed_bytes);
+        }
         if (flags & kErrHashFull) {
             drop();
             return fail(ctx, GSPAN_ERR_CUDA, "edge index: a probe ran through the table");

@@ -1023,7 +1023,8 @@ __global__ void k_segments(int32_t n, int32_t m, int32_t lwin, int32_t K, int32_
 // entries is inserted (linear probing, bounded by the table size).
 __global__ void k_entry_flags(int32_t m, const int32_t* __restrict__ src, const int32_t* __restrict__ offsets,
                               const uint64_t* __restrict__ adj, const int32_t* __restrict__ vrank,
-                              uint32_t* __restrict__ selfloop, int32_t* __restrict__ rev,
+                              const int32_t* __restrict__ segstart, const int32_t* __restrict__ win_base,
+                              int32_t lwin, int32_t K, uint32_t* __restrict__ selfloop, int32_t* __restrict__ rev,
                               unsigned long long* __restrict__ eidx, uint32_t cap, uint32_t* status)
 {
     bool asym = false, loop = false, parallel = false, full = false;
@@ -1054,7 +1055,19 @@ __global__ void k_entry_flags(int32_t m, const int32_t* __restrict__ src, const 
         int32_t r0 = (int32_t)i;
         while (r0 > bu && adj[r0 - 1] == ent) --r0;
         const uint64_t rk = pack_entry(entry_el(ent), (uint32_t)vrank[u], u);
-        const int32_t b = offsets[x], e = offsets[x + 1];
+        int32_t b = offsets[x], e = offsets[x + 1];
+        if (segstart) {
+            // The reverse entry lies in x's segment of (edge label, u's label):
+            // search that segment only.
+            const int32_t local = vrank[u] - win_base[vrank[x]];
+            if ((uint32_t)local < (uint32_t)lwin) {
+                const int64_t so = (int64_t)x * (K + 1) + (int64_t)entry_el(ent) * lwin + local;
+                b = segstart[so];
+                e = segstart[so + 1];
+            } else {
+                e = b;
+            }
+        }
         const int32_t q = lower_bound_entry(adj, b, e, rk) + ((int32_t)i - r0);
         const bool found = q < e && adj[q] == rk;
         rev[i] = found ? q : -1;
@@ -2050,7 +2063,8 @@ cudaError_t launch_expand(const ExpandArgs& x, Pass pass, cudaStream_t st)
 cudaError_t launch_entry_flags(DevGraph& g, uint32_t* status, cudaStream_t st)
 {
     if (g.m == 0) return cudaSuccess;
-    k_entry_flags<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj, g.vrank, g.selfloop, g.rev,
+    k_entry_flags<<<grid_for(g.m, 256), 256, 0, st>>>(g.m, g.src, g.offsets, g.adj, g.vrank, g.segstart, g.win_base,
+                                                      g.lwin, g.nel * g.lwin, g.selfloop, g.rev,
                                                       reinterpret_cast<unsigned long long*>(g.eidx), g.eidx_cap,
                                                       status);
     return cudaGetLastError();
