@@ -208,6 +208,13 @@ struct ParentMeta {
     int32_t gen_kc;
     // 2^32 rows or more: the row pass checks its 32-bit counters for a wrap.
     int32_t r_wide;
+    // One edge label (entry-column row walk): per source, the pattern vertices
+    // the walk visits, in label order - labels inside the source's valid
+    // range and, without self-loops, not the source itself - packed as
+    // j | (code edge joining j and the source + 1) << 4 | (that edge starts at
+    // the source) << 8 | label rank << 16.
+    int8_t walk_n[kMaxV];
+    int32_t walk[kMaxV][kMaxV];
 };
 
 // Per-level key space arrays on the device.

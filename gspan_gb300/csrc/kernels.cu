@@ -1202,12 +1202,17 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
             // Vertices are visited in label order, so each label's hits
             // are summed on the fly: a segment is lost to the row when
             // its images fill all of it.
+            // The walk (see ParentMeta::walk) holds only the vertices that
+            // can hit: one load per vertex, the static filters done on the host.
             const int vs = P.src_v[s];
+            const int nwalk = P.walk_n[s];
+            const int32_t* const walk = P.walk[s];
             int cur_t = -1, gstart = 0;
             int32_t hits = 0, minlb = e, maxub = b;
-            for (int oi = 0; oi <= nv; ++oi) {
-                const int j = oi < nv ? P.lorder[oi] : 0;
-                const int t = oi < nv ? P.vlab[j] : -1;
+            for (int oi = 0; oi <= nwalk; ++oi) {
+                const int32_t wk = oi < nwalk ? walk[oi] : 0;
+                const int j = wk & 15;
+                const int t = oi < nwalk ? (wk >> 16) & 0xFFFF : -1;
                 if (t != cur_t) {
                     if (hits > 0) {
                         const uint32_t kc = (uint32_t)(cur_t - P.lbase);
@@ -1233,25 +1238,22 @@ __device__ __forceinline__ void mask_row(const MaskDev& a, const ParentMeta& P, 
                     minlb = e;
                     maxub = b;
                 }
-                if (oi == nv) break;
+                if (oi == nwalk) break;
                 const uint64_t seg0 = pack_entry(0, (uint32_t)t, 0);
-                if (t < min_label || seg0 < lo) continue;
                 const int32_t x = img[j];
                 if (a.loops) {
                     // Images may repeat: one hit per distinct image (equal
                     // images have equal labels, so within the group).
                     bool dup = false;
-                    for (int q = gstart; q < oi; ++q) dup |= img[P.lorder[q]] == x;
+                    for (int q = gstart; q < oi; ++q) dup |= img[walk[q] & 15] == x;
                     if (dup) continue;
-                } else if (j == vs) {
-                    continue;   // no self-loops: the source is not its own neighbour
                 }
                 const uint64_t key = seg0 | (uint32_t)x;
-                const int jj = P.pair_edge[s][j];
+                const int jj = ((wk >> 4) & 15) - 1;
                 int32_t pos = -1;
                 if (jj >= 0) {
                     const int32_t stored = ecol(jj);
-                    pos = P.e_from[jj] == vs ? stored : __ldg(a.rev + stored);
+                    pos = (wk >> 8) & 1 ? stored : __ldg(a.rev + stored);
                     // The entry column holds the image edge's entry (or, from its
                     // other end, the reverse entry): inside u's list it is the key.
                     if (pos < b || pos >= e) pos = -1;

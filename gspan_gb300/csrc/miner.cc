@@ -673,6 +673,23 @@ struct Run {
                 for (const CodeEdge& e : c)
                     if (e.el < 32 && ((e.from == P.vn && e.to == P.back_v[t]) || (e.to == P.vn && e.from == P.back_v[t])))
                         P.back_used[t] |= 1u << e.el;
+            for (int s2 = 0; s2 < P.nsrc; ++s2) {
+                const int vs = P.src_v[s2];
+                const int lo_el = s2 == 0 ? 0 : P.src_el[s2];
+                const int lo_tl = s2 == 0 ? P.min_label : P.src_tl[s2];
+                int n = 0;
+                for (int oi = 0; oi < nv; ++oi) {
+                    const int j = P.lorder[oi];
+                    const int t = P.vlab[j];
+                    // Segment (edge label 0, t) at or above the source's lower bound.
+                    if (t < P.min_label || !(0 > lo_el || (0 == lo_el && t >= lo_tl))) continue;
+                    if (!g.loops && j == vs) continue;
+                    const int jj = P.pair_edge[s2][j];
+                    const int from_vs = jj >= 0 && P.e_from[jj] == vs ? 1 : 0;
+                    P.walk[s2][n++] = j | ((jj + 1) << 4) | (from_vs << 8) | (t << 16);
+                }
+                P.walk_n[s2] = (int8_t)n;
+            }
             P.row_begin = parents[i].row_begin;
             P.row_end = parents[i].row_end;
             if (gen) {
