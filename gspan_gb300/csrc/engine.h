@@ -335,7 +335,7 @@ cudaError_t launch_mask_rows(const MaskArgs& a, cudaStream_t st);
 // Two-level last step: the row pass over rows generated from gen_parents'
 // rows (every parent has gen_kind != 0), none of them stored.
 cudaError_t launch_mask_gen(const MaskArgs& a, cudaStream_t st);
-// Prefix of the touched lists, then the sweep (two launches).
+// Touched lists from R, their prefix, then the sweep (three launches).
 cudaError_t launch_mask_sweep(const MaskArgs& a, cudaStream_t st);
 // Domain sizes of the group's tuples from its mask planes (after the sweep).
 cudaError_t launch_mask_popcount(const MaskArgs& a, cudaStream_t st);

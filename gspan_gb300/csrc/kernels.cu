@@ -920,12 +920,13 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(ExpandDev a)
 // R[u] - H[e], and the new vertex's domain is {to(e) : R[u] > H[e]}.  An old
 // vertex p's domain for (s, c) is {img_r(p) : row r has an entry of
 // seg(u_r, c) outside its images}; the row pass ORs the set of such c (a
-// bitmask over the tuple space) into M[p][img_r(p)].  Domain sizes are counted
-// as bits first appear in M, so no pass over M is needed.  All of it is exact.
+// bitmask over the tuple space) into M[p][img_r(p)], the sweep the new
+// vertex's bits, and k_mask_popcount counts the set bits of every mask plane
+// into the domain sizes afterwards.  All of it is exact.
 //
-// The row pass lists every vertex whose R goes 0 -> 1 (`touched`), so the
-// sweep visits only those vertices; it also resets the R and H entries it
-// reads, leaving both arrays zero for the next group of parents.
+// k_mask_touched lists every vertex with a non-zero R (`touched`), so the
+// sweep visits only those vertices; the sweep also resets the R and H entries
+// it reads, leaving both arrays zero for the next group of parents.
 
 constexpr int kMaskWarps = 8;
 // Pattern vertices whose mask words the row pass reads together (one word each).
