@@ -46,3 +46,16 @@ def test_reference_arm_loads_no_native_library():
 def test_reference_arm_unavailable_where_the_port_cannot_run():
     line = run_bench("--impl", "reference", "--workload", "chung_lu_3_7m")
     assert line["impl"] == "reference" and "unavailable" in line
+
+
+def test_hbm_peak_fallback(tmp_path, monkeypatch):
+    """The roofline denominator comes from MEASURED_PEAKS.json when it is
+    there and falls back to the earlier GB300 measurement, labelled, when not."""
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    peak, source = bench.hbm_peak()
+    assert peak == 6800.0 and source.startswith("fallback")
+    (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"hbm_gbs": 7000.5}))
+    peak, source = bench.hbm_peak()
+    assert peak == 7000.5 and "measured" in source
