@@ -686,7 +686,8 @@ struct Run {
                     if (!g.loops && j == vs) continue;
                     const int jj = P.pair_edge[s2][j];
                     const int from_vs = jj >= 0 && P.e_from[jj] == vs ? 1 : 0;
-                    P.walk[s2][n++] = j | ((jj + 1) << 4) | (from_vs << 8) | (t << 16);
+                    P.walk[s2][n++] = (int32_t)((uint32_t)j | ((uint32_t)(jj + 1) << 4) | ((uint32_t)from_vs << 8) |
+                                                ((uint32_t)t << 16));
                 }
                 P.walk_n[s2] = (int8_t)n;
             }
