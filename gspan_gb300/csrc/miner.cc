@@ -386,6 +386,7 @@ struct Run {
             aclr.add(as.pool + bitmap_words, (int64_t)hash_words, 0xFFFFFFFFu);
             aclr.add(as.d_cursor, (int64_t)act.size() * 2);
             GS_CK(launch_clear(aclr, s), "clear launch");
+            st.kernel_launches += aclr.n > 0;
         }
         if (materialize && out_rows > 0) {
             // One entry column (the seed's entry) follows the vertex columns.
@@ -918,6 +919,7 @@ struct Run {
                       c.add(ctx->d_counters + 2, 2)))
                     return fail(ctx, GSPAN_ERR_CUDA, "clear list full");
                 GS_CK(launch_clear(c, s), "clear launch");
+                st.kernel_launches += c.n > 0;
                 c.n = 0;
                 MaskArgs ma{};
                 ma.g = &g;
@@ -962,7 +964,8 @@ struct Run {
                 tic(&e0, &e1);
                 GS_CK(launch_mask_popcount(ma, s), "mask popcount launch");
                 toc(e0, e1, &st.domain_ms);
-                st.kernel_launches += 4;
+                // Row pass, touched lists, their prefix, sweep, popcount.
+                st.kernel_launches += 5;
                 st.rows_launches += 1;
             }
             st.rows_bytes += rows_bytes;
@@ -977,6 +980,7 @@ struct Run {
         x.scanned = ctx->d_counters + 1;
         x.status = ctx->d_status;
         GS_CK(launch_clear(clr, s), "clear launch");   // no-op when a mask group took the list
+        st.kernel_launches += clr.n > 0;
         if (!cg.empty()) {
             GS_CK(dalloc(&d_cg, cg.size(), s), "alloc parents");
             GS_CK(copy(d_cg, cg.data(), cg.size() * sizeof(ParentMeta), cudaMemcpyHostToDevice, s), "copy parents");
@@ -1231,6 +1235,7 @@ struct Run {
             mclr.add(d_cur, (int64_t)freq.size() * 2);
             mclr.add(ctx->d_counters, 4);
             GS_CK(launch_clear(mclr, s), "clear launch");
+            st.kernel_launches += mclr.n > 0;
         }
         x.parents = d_all;
         x.parents_h = all.data();
